@@ -1,0 +1,377 @@
+"""Benchmark: the in-HBM suite on RMAT scale 24 (the reference engine's plain
+per-algorithm entry points, GB300 path), GTEPS.
+
+Workload (one step): on an undirected RMAT graph, scale 24 (16.8M vertices),
+edge factor 16, a/b/c/d = .57/.19/.19/.05, seed 2, self-loops and duplicates
+removed, uint32 CSR, uint32 weights uniform in [1, 63]:
+  * BFS from 64 seeded random non-isolated sources,
+  * SSSP from the first 4 of those sources,
+  * CC to min-vertex labels,
+  * PageRank, damping 0.85, 20 iterations (FP32).
+TEPS convention (Graph500): BFS/SSSP count the undirected edges of the
+searched component, CC counts m/2, PageRank 20 * m/2.  value = suite edges /
+suite device time (CUDA events on the engine's stream; inputs resident in
+HBM, outputs left on the device).  e2e = the same through the C ABI with
+host buffers: CSR upload from pinned host memory, every result read back.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "test-world_gb300"))
+
+PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--scale", type=int, default=24)
+    p.add_argument("--sources", type=int, default=64)
+    p.add_argument("--sssp-sources", type=int, default=4)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_init(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t[0])
+
+
+def sum_over_ranks(pg, x):
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t[0])
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.samples.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for s in self.samples:
+            try:
+                sm.append(float(s[1]))
+                smax = float(s[2])
+                for k, name in enumerate(names):
+                    if s[5 + k].lower() == "active":
+                        reasons.add(name)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_workload(args):
+    import ptgraph
+    t0 = time.time()
+    off, col, w = ptgraph.gen_rmat(args.scale, 16, 0.57, 0.19, 0.19, seed=2, symmetric=True, wmin=1, wmax=63)
+    gen_s = time.time() - t0
+    n, m = off.size - 1, col.size
+    deg = np.diff(off.astype(np.int64))
+    rng = np.random.default_rng(2)
+    sources = rng.choice(np.nonzero(deg)[0], args.sources, replace=False).astype(np.uint32)
+    return off, col, w, deg, sources, gen_s
+
+
+def teps_edges(levels, deg):
+    """Undirected edges in the searched component (Graph500): sum of degrees of reached vertices / 2."""
+    reached = levels != 0xFFFFFFFF
+    return int(deg[reached].sum()) // 2
+
+
+def run_reference(args, rank, pg):
+    """The reference's algorithm on host cores (the oracle's multithreaded restatement)."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    off, col, w, deg, sources, _ = make_workload(args)
+    threads = os.cpu_count() or 1
+    m = col.size
+    times, edges = [], []
+    for step in range(args.warmup + args.steps):
+        s = int(sources[step % sources.size])
+        t0 = time.perf_counter()
+        lv = O.mt_bfs(off, col, s, threads)
+        d = O.mt_sssp(off, col, w, s, threads)
+        O.mt_cc(off, col, threads)
+        O.mt_pagerank(off, col, threads, iters=2)
+        dt = time.perf_counter() - t0
+        e = 2 * teps_edges(lv, deg) + m // 2 + 2 * (m // 2)
+        if step >= args.warmup:
+            times.append(dt)
+            edges.append(e)
+    val = sum(edges) / sum(times) / 1e9
+    sample = "per step: 1 BFS + 1 SSSP (sources cycling over the 64) + CC + 2 PageRank iterations"
+    line = {"impl": "reference", "metric": "suite_gteps", "value": val, "unit": "GTEPS", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+            "data": "synthetic", "config": workload_config(args),
+            "cpu_baseline": {"value": val, "unit": "GTEPS", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": val, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def workload_config(args):
+    return {"workload": "in-HBM suite: RMAT scale %d ef16 a.57 b.19 c.19 seed 2 symmetric u32 CSR w[1,63]; "
+                        "BFS x%d sources, SSSP x%d, CC, PageRank 20 it" % (args.scale, args.sources,
+                                                                            args.sssp_sources),
+            "scale": args.scale, "edge_factor": 16, "bfs_sources": args.sources,
+            "sssp_sources": args.sssp_sources, "pagerank_iterations": 20,
+            "l2": "inputs larger than L2 (CSR ~4.4 GB vs 129 MB L2); no flush"}
+
+
+def main():
+    args = parse()
+    rank, world, local, pg = dist_init(args)
+    if args.impl == "reference":
+        run_reference(args, rank, pg)
+        return
+    import torch
+    import ptgraph
+    torch.cuda.set_device(local)
+    ctx = ptgraph.Ctx(local)
+    off, col, w, deg, sources, gen_s = make_workload(args)
+    n, m = off.size - 1, col.size
+    off32 = off.astype(np.uint32)
+    G = ctx.graph(off32, col, w, symmetric=True)
+    dev = {k: torch.empty(n, dtype=torch.int32, device="cuda") for k in ("bfs", "sssp", "cc")}
+    dev["pr"] = torch.empty(n, dtype=torch.float32, device="cuda")
+
+    # edges per step (TEPS convention), from one collected pass
+    G_bfs_edges = []
+    for s in sources:
+        lv = G.bfs(int(s))
+        G_bfs_edges.append(teps_edges(lv, deg))
+    step_edges = sum(G_bfs_edges) + sum(G_bfs_edges[:args.sssp_sources]) + m // 2 + 20 * (m // 2)
+
+    def step_device():
+        dms = 0.0
+        for i, s in enumerate(sources):
+            st = {}
+            G.bfs(int(s), flags=ptgraph.PTG_OUT_DEVICE, stats=st, out=dev["bfs"])
+            dms += st["device_ms"]
+        for s in sources[:args.sssp_sources]:
+            st = {}
+            G.sssp(int(s), flags=ptgraph.PTG_OUT_DEVICE, stats=st, out=dev["sssp"])
+            dms += st["device_ms"]
+        st = {}
+        G.cc(flags=ptgraph.PTG_OUT_DEVICE, stats=st, out=dev["cc"])
+        dms += st["device_ms"]
+        st = {}
+        G.pagerank(flags=ptgraph.PTG_OUT_DEVICE, stats=st, out=dev["pr"])
+        dms += st["device_ms"]
+        return dms
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    barrier(pg)
+    launches0 = ctx.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    t0 = time.perf_counter()
+    dev_ms = [step_device() for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clock_info = clocks.stop()
+    barrier(pg)
+    launches = ctx.launch_count() - launches0
+    ms_per_step = max_over_ranks(pg, sum(dev_ms) / len(dev_ms))
+    total_edges = sum_over_ranks(pg, step_edges)
+    value = total_edges / (ms_per_step / 1e3) / 1e9
+
+    # per-kernel profile of one step (separate pass, not part of the timed value)
+    ctx.profile(True)
+    step_device()
+    prof = ctx.profile_entries()
+    ctx.profile(False)
+    per_alg = {}
+    st = {}
+    G.bfs(int(sources[0]), flags=ptgraph.PTG_OUT_DEVICE, stats=st, out=dev["bfs"])
+    per_alg["bfs_ms_src0"] = st["device_ms"]
+    roof = roofline(prof, n, m, step_edges, G_bfs_edges, args)
+
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_measure(ctx, off32, col, w, sources, args, deg, step_edges, n, m)
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(off, col, w, sources, deg, m)
+    if rank == 0:
+        line = {"metric": "suite_gteps", "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_per_step, "wall_ms_per_step": 1e3 * wall / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+                "data": "synthetic (RMAT generated on the host, seeded)", "config": workload_config(args),
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches // args.steps,
+                "clocks": clock_info, "kernel_profile_ms": {k: [c, round(t, 4)] for k, (c, t) in prof.items()},
+                "graph": {"n": n, "m": m, "gen_s": round(gen_s, 2)}}
+        print(json.dumps(line))
+
+
+def peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def roofline(prof, n, m, step_edges, bfs_edges, args):
+    """Roofline of the dominant kernel: algorithmic bytes per launch / its average launch time."""
+    hbm, kind = peaks()
+    top = max(prof.items(), key=lambda kv: kv[1][1])
+    name, (cnt, tot) = top
+    avg_ms = tot / max(cnt, 1)
+    if name == "k_spmv":
+        per_launch = 4 * (n + 1) + 8 * m + 8 * n  # one PageRank iteration
+        unit_desc = "PageRank iteration: 4(n+1) + 8m + 8n bytes"
+    else:
+        per_launch = None
+        unit_desc = "no algorithmic byte model for %s yet" % name
+    achieved = per_launch / (avg_ms / 1e3) / 1e9 if per_launch else None
+    return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": hbm, "peak_kind": kind,
+            "unit": "GB/s", "frac": achieved / hbm if achieved else None, "traffic": None,
+            "bytes_per_launch": per_launch, "avg_launch_ms": avg_ms, "launches": cnt, "model": unit_desc,
+            "share_of_step": tot / sum(v[1] for v in prof.values())}
+
+
+def e2e_measure(ctx, off32, col, w, sources, args, deg, step_edges, n, m):
+    import torch
+    import ptgraph
+    # pinned host copies of the inputs
+    ph = {}
+    for k, a in (("off", off32), ("col", col), ("w", w)):
+        t = torch.empty(a.size, dtype=torch.int32, pin_memory=True)
+        t.numpy().view(a.dtype)[:] = a
+        ph[k] = t.numpy().view(a.dtype)
+    outs = {"bfs": torch.empty(n, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32),
+            "sssp": torch.empty(n, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32),
+            "cc": torch.empty(n, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32),
+            "pr": torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()}
+
+    def step():
+        G = ctx.graph(ph["off"], ph["col"], ph["w"], symmetric=True, pinned=True)
+        for s in sources:
+            G.bfs(int(s), out=outs["bfs"])
+        for s in sources[:args.sssp_sources]:
+            G.sssp(int(s), out=outs["sssp"])
+        G.cc(out=outs["cc"])
+        G.pagerank(out=outs["pr"])
+        G.close()
+
+    for _ in range(min(2, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    k = max(1, min(3, args.steps))
+    t0 = time.perf_counter()
+    for _ in range(k):
+        step()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / k
+    h2d = off32.nbytes + col.nbytes + w.nbytes
+    d2h = 4 * n * (len(sources) + args.sssp_sources + 2)
+    return {"value": step_edges / dt / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3,
+            "path": "ptg_graph_create from pinned host CSR + ptg_bfs/sssp/cc/pagerank into host buffers"}
+
+
+def cpu_baseline(off, col, w, sources, deg, m):
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    s = int(sources[0])
+    t0 = time.perf_counter()
+    lv = O.mt_bfs(off, col, s, threads)
+    t_bfs = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.mt_sssp(off, col, w, s, threads)
+    t_sssp = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.mt_cc(off, col, threads)
+    t_cc = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.mt_pagerank(off, col, threads, iters=2)
+    t_pr = time.perf_counter() - t0
+    e = teps_edges(lv, deg)
+    edges = 2 * e + m // 2 + 2 * (m // 2)
+    tot = t_bfs + t_sssp + t_cc + t_pr
+    return {"value": edges / tot / 1e9, "unit": "GTEPS", "cores": threads, "kind": "port",
+            "sample": "1 BFS + 1 SSSP (source 0 of 64) + CC + 2 PageRank iterations on the same graph",
+            "seconds": {"bfs": t_bfs, "sssp": t_sssp, "cc": t_cc, "pr2": t_pr}}
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,392 @@
+/*
+ * ptgraph.h - C ABI of the GB300-native out-of-GPU-memory graph engine.
+ *
+ * Two layers are exported:
+ *
+ *  1. Drop-in entry points with the reference's names and parameter lists
+ *     (ptGraph/main.cu:24-56).  Each takes a host CSR in the reference's
+ *     "n offsets, no sentinel" form (the last vertex's degree is
+ *     m - offsets[n-1], ptGraph/main.cu:1220), runs the algorithm on the GPU
+ *     and returns the elapsed milliseconds, as the reference does.  Unlike the
+ *     reference they keep the result: ptg_compat_last_result() copies it out.
+ *     Errors never exit(): they return -1 and ptg_compat_last_error() says why.
+ *
+ *  2. The engine API (ptg_*): a context per device, an uploaded graph handle
+ *     whose edge array is either resident in HBM or split into partitions that
+ *     stream from pinned host memory, per-algorithm entry points with
+ *     caller-owned outputs, batched and served queries.  Every call returns a
+ *     ptg_status; no call exits the process.
+ *
+ * Value conventions follow the reference by default:
+ *   BFS  : level[src] = 1, level[v] = hops + 1, unreached = 0xFFFFFFFF
+ *          (ptGraph/main.cu:1239-1246, ptGraph/gpu_kernels.cu:118-134)
+ *   SSSP : dist[src] = 1, dist[v] = 1 + sum of weights, unreached = 0xFFFFFFFF
+ *          (ptGraph/main.cu:740-746, ptGraph/gpu_kernels.cu:152-172); the
+ *          UM-only reference variant uses 0xFFFFFFFE for unreached
+ *          (ptGraph/main.cu:584-588), selected by PTG_UNREACHED_MINUS1.
+ *   CC   : label[v] = min vertex id over the vertices that reach v through
+ *          out-edges (ptGraph/main.cu:283-286, ptGraph/gpu_kernels.cu:136-150);
+ *          on a symmetric graph that is the min id of v's component.
+ *   PR   : the reference has none (ptGraph/main.cu:937 is commented out);
+ *          pull PageRank, damping d, r0 = 1/n, dangling mass spread uniformly,
+ *          fixed iteration count, FP32 ranks with FP64 per-vertex sums.
+ */
+#ifndef PTGRAPH_H
+#define PTGRAPH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PTG_VERSION_MAJOR 0
+#define PTG_VERSION_MINOR 1
+
+/* ------------------------------------------------------------------------ */
+/* Status codes.  The reference only has gpuAssert -> exit(code)            */
+/* (ptGraph/main.cu:15-22); here every failure is a return value.           */
+/* ------------------------------------------------------------------------ */
+typedef enum ptg_status {
+    PTG_OK = 0,
+    PTG_ERR_INVALID = 1,     /* bad argument: null pointer, src >= n, malformed CSR */
+    PTG_ERR_OOM = 2,         /* device or pinned host allocation failed            */
+    PTG_ERR_CUDA = 3,        /* a CUDA runtime call failed                          */
+    PTG_ERR_TIMEOUT = 4,     /* a bounded device-side wait ran out                  */
+    PTG_ERR_UNSUPPORTED = 5, /* option not supported for this graph                 */
+    PTG_ERR_NO_DEVICE = 6,   /* no CUDA device visible                              */
+    PTG_ERR_CANCELLED = 7,   /* served request cancelled before it ran              */
+    PTG_ERR_BUSY = 8         /* server queue full                                   */
+} ptg_status;
+
+const char *ptg_status_string(ptg_status s);
+
+/* Reference edge record for weighted graphs (ptGraph/globals.cuh:2-5). */
+typedef struct ptg_edge_w {
+    uint32_t to;
+    uint32_t weight;
+} ptg_edge_w;
+
+/* ------------------------------------------------------------------------ */
+/* CSR description (input side; caller owns every array).                   */
+/* Replaces the (uint testNumNodes, uint testNumEdge, uint *nodePointersI,  */
+/* uint *edgeList | EdgeWithWeight *edgeList) tuple (ptGraph/main.cu:32-52) */
+/* and lifts its 32-bit limits: n and m are 64-bit, offsets may be u64.     */
+/* ------------------------------------------------------------------------ */
+enum {
+    PTG_OFFSETS_U32 = 0,
+    PTG_OFFSETS_U64 = 1
+};
+enum {
+    PTG_FORM_SENTINEL = 0,  /* offsets has n+1 entries, offsets[n] == m          */
+    PTG_FORM_REFERENCE = 1  /* offsets has n entries (ptGraph/main.cu:97-121)    */
+};
+enum {
+    PTG_CSR_SYMMETRIC = 1u << 0, /* every edge u->v has v->u: enables pull/bottom-up
+                                    BFS, hooking CC and pull PageRank on the same CSR */
+    PTG_CSR_HOST_PINNED = 1u << 1 /* arrays already pinned (no registration needed) */
+};
+
+typedef struct ptg_csr {
+    uint64_t n;                  /* vertices                                    */
+    uint64_t m;                  /* directed edges                              */
+    const void *offsets;         /* u32 or u64, n or n+1 entries (see form)     */
+    uint32_t offset_type;        /* PTG_OFFSETS_U32 / PTG_OFFSETS_U64           */
+    uint32_t offset_form;        /* PTG_FORM_SENTINEL / PTG_FORM_REFERENCE      */
+    const uint32_t *col;         /* [m] targets (SoA); may be NULL if edges_aos */
+    const uint32_t *weight;      /* [m] weights (SoA); optional                 */
+    const ptg_edge_w *edges_aos; /* [m] reference AoS records; optional         */
+    uint32_t flags;              /* PTG_CSR_*                                   */
+    uint32_t reserved;
+} ptg_csr;
+
+/* ------------------------------------------------------------------------ */
+/* Partition configuration.  Replaces the reference's global fragment_size  */
+/* (ptGraph/main.cu:66) and its per-function memory fractions               */
+/* frac*(totalGlobalMem - 40n)/sizeof(edge) (ptGraph/main.cu:237, 694,      */
+/* 1193, 1433, 1693, 2077, 2213).                                           */
+/* ------------------------------------------------------------------------ */
+enum {
+    PTG_RESIDENT_PREFIX = 0, /* lowest-numbered partitions stay in HBM (the
+                                reference's static prefix, main.cu:1222-1232) */
+    PTG_RESIDENT_NONE = 1,   /* stream every partition (tests the swapper)     */
+    PTG_RESIDENT_HOT = 2     /* promote partitions by visit count
+                                (gpu_kernels.cu:254-282, 475-485)              */
+};
+
+typedef struct ptg_partition_config {
+    uint64_t partition_bytes;     /* edge bytes per streamed partition; 0 = 256 MiB   */
+    uint64_t device_budget_bytes; /* bytes of HBM for resident edges; 0 = use frac   */
+    double device_frac;           /* fraction of free HBM for resident edges; 0 = 0.9 */
+    uint32_t n_staging_buffers;   /* 2 or 3 (double/triple buffering); 0 = 2          */
+    uint32_t resident_policy;     /* PTG_RESIDENT_*                                   */
+    uint32_t force_out_of_core;   /* 1 = partition even if the graph fits             */
+    uint32_t hot_threshold;       /* PTG_RESIDENT_HOT promotion threshold (visits)    */
+} ptg_partition_config;
+
+void ptg_partition_config_default(ptg_partition_config *cfg);
+
+/* ------------------------------------------------------------------------ */
+/* Per-run options and statistics.                                          */
+/* ------------------------------------------------------------------------ */
+enum {
+    PTG_OUT_DEVICE = 1u << 0,        /* output pointer is device memory            */
+    PTG_LEVEL_ZERO_BASED = 1u << 1,  /* BFS/SSSP: source value 0 instead of 1      */
+    PTG_UNREACHED_MINUS1 = 1u << 2,  /* unreached = 0xFFFFFFFE (main.cu:584-588)   */
+    PTG_NO_DIRECTION_OPT = 1u << 3,  /* BFS: top-down only                         */
+    PTG_REFERENCE_SCHEDULE = 1u << 4 /* BFS/SSSP/CC: the reference's frontier
+                                        label-propagation schedule (every improved
+                                        vertex re-expanded next round)             */
+};
+
+typedef struct ptg_run_stats {
+    uint32_t iterations;        /* frontier rounds (BFS levels, SSSP rounds, ...)  */
+    uint32_t bottom_up_rounds;  /* BFS rounds run bottom-up                        */
+    uint64_t edges_relaxed;     /* edges inspected by relax kernels                */
+    uint64_t vertices_reached;  /* vertices with a finite value                    */
+    uint64_t edges_in_component;/* directed edges out of reached vertices          */
+    uint64_t link_bytes;        /* bytes streamed host->device by the swapper      */
+    uint64_t partitions_streamed;
+    uint64_t partitions_skipped;/* streamed partitions skipped as inactive         */
+    double device_ms;           /* GPU time of the run (CUDA events)              */
+    double link_ms;             /* time the copy stream was busy                   */
+} ptg_run_stats;
+
+typedef struct ptg_run_opts {
+    uint32_t flags;             /* PTG_OUT_DEVICE | PTG_LEVEL_ZERO_BASED | ...     */
+    uint32_t delta;             /* SSSP near/far bucket width; 0 = auto            */
+    uint32_t max_iterations;    /* 0 = n + 1                                       */
+    uint32_t reserved;
+    ptg_run_stats *stats;       /* optional                                        */
+} ptg_run_opts;
+
+typedef struct ptg_pr_opts {
+    uint32_t flags;             /* PTG_OUT_DEVICE                                  */
+    uint32_t iterations;        /* 0 = 20                                          */
+    double damping;             /* 0 = 0.85                                        */
+    ptg_run_stats *stats;
+} ptg_pr_opts;
+
+/* ------------------------------------------------------------------------ */
+/* Context and graph handles.                                               */
+/* ------------------------------------------------------------------------ */
+typedef struct ptg_ctx ptg_ctx;
+typedef struct ptg_graph ptg_graph;
+
+ptg_status ptg_ctx_create(int device, ptg_ctx **out);
+void ptg_ctx_destroy(ptg_ctx *ctx);
+/* Message of the last failure on this context (thread-safe per context). */
+const char *ptg_ctx_last_error(const ptg_ctx *ctx);
+/* Device properties the engine sized itself for. */
+ptg_status ptg_ctx_device_info(const ptg_ctx *ctx, int *sm_count, uint64_t *hbm_bytes,
+                               uint64_t *free_bytes);
+
+/* Kernel accounting.  Every kernel the engine launches is counted; with
+ * profiling enabled each launch is also bracketed by CUDA events on the
+ * stream it runs on and its device time is summed per kernel name.
+ * Enabling (or disabling) clears the per-kernel totals. */
+ptg_status ptg_ctx_profile_enable(ptg_ctx *ctx, int enable);
+uint64_t ptg_ctx_launch_count(const ptg_ctx *ctx);
+uint32_t ptg_ctx_profile_entries(const ptg_ctx *ctx);
+ptg_status ptg_ctx_profile_entry(const ptg_ctx *ctx, uint32_t i, const char **name,
+                                 uint64_t *launches, double *total_ms);
+
+/* Upload a CSR.  Edges live in HBM when they fit the budget; otherwise the
+ * first partitions stay resident and the rest stream from pinned host memory
+ * (the caller's arrays are registered, not copied).  The caller's arrays must
+ * outlive the graph when it is out of core. */
+ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partition_config *cfg,
+                            ptg_graph **out);
+void ptg_graph_destroy(ptg_graph *g);
+
+typedef struct ptg_graph_info {
+    uint64_t n, m;
+    uint32_t symmetric;
+    uint32_t weighted;
+    uint32_t out_of_core;
+    uint32_t offsets_u64;
+    uint64_t partitions;          /* total edge partitions                        */
+    uint64_t resident_partitions; /* partitions kept in HBM                       */
+    uint64_t partition_edges;     /* edges per partition                          */
+    uint64_t resident_edges;      /* edges in HBM                                 */
+    uint64_t device_bytes;        /* HBM held by the graph                        */
+} ptg_graph_info;
+ptg_status ptg_graph_info_get(const ptg_graph *g, ptg_graph_info *info);
+
+/* Host-only partition planner (no GPU needed): how a graph with these offsets
+ * is cut for a given budget.  part_first_vertex[p] is the first vertex whose
+ * adjacency overlaps partition p (array of *num_partitions entries, may be NULL
+ * to query the count). */
+ptg_status ptg_plan_partitions(uint64_t n, uint64_t m, const uint64_t *offsets_n1,
+                               uint64_t bytes_per_edge, const ptg_partition_config *cfg,
+                               uint64_t device_free_bytes, uint64_t *num_partitions,
+                               uint64_t *resident_partitions, uint64_t *partition_edges,
+                               uint64_t *part_first_vertex);
+
+/* ------------------------------------------------------------------------ */
+/* Single-query algorithms (bfsCaculateIn*, ssspCaculateIn*, ccCaculateIn*,  */
+/* prCaculateIn* of ptGraph/main.cu:24-56).                                 */
+/* Output arrays have n entries and are host memory unless PTG_OUT_DEVICE.  */
+/* ------------------------------------------------------------------------ */
+ptg_status ptg_bfs(ptg_graph *g, uint32_t src, uint32_t *levels, const ptg_run_opts *opts);
+ptg_status ptg_sssp(ptg_graph *g, uint32_t src, uint32_t *dist, const ptg_run_opts *opts);
+ptg_status ptg_cc(ptg_graph *g, uint32_t *labels, const ptg_run_opts *opts);
+ptg_status ptg_pagerank(ptg_graph *g, float *rank, const ptg_pr_opts *opts);
+/* Personalized PageRank: teleport (and dangling mass) to src, r0 = e_src. */
+ptg_status ptg_ppr(ptg_graph *g, uint32_t src, float *rank, const ptg_pr_opts *opts);
+
+/* ------------------------------------------------------------------------ */
+/* Batched queries.                                                          */
+/* ------------------------------------------------------------------------ */
+/* Multi-source BFS / SSSP: k sources, 64 per bitmask word.  out is k*n,
+ * source-major (out[i*n + v] is the value of v for sources[i]); the values
+ * equal k separate ptg_bfs / ptg_sssp calls. */
+ptg_status ptg_msbfs(ptg_graph *g, const uint32_t *sources, uint32_t k, uint32_t *out,
+                     const ptg_run_opts *opts);
+ptg_status ptg_mssssp(ptg_graph *g, const uint32_t *sources, uint32_t k, uint32_t *out,
+                      const ptg_run_opts *opts);
+
+/* Connected components of many independent symmetric graphs in one
+ * persistent launch.  Graph i has vertices [vtx_begin[i], vtx_begin[i+1]) of a
+ * concatenated CSR (offsets are global u64 with sentinel, col holds global
+ * vertex ids).  labels[v] = smallest vertex id of v's component, in LOCAL
+ * numbering (global id - vtx_begin[i]). */
+ptg_status ptg_cc_batch(ptg_ctx *ctx, uint32_t num_graphs, const uint64_t *vtx_begin,
+                        const uint64_t *offsets, const uint32_t *col, uint32_t *labels,
+                        const ptg_run_opts *opts);
+
+/* ------------------------------------------------------------------------ */
+/* Serving: a request loop with continuous batching.                        */
+/* ------------------------------------------------------------------------ */
+typedef struct ptg_server ptg_server;
+
+enum { PTG_Q_BFS = 0, PTG_Q_SSSP = 1, PTG_Q_PPR = 2 };
+
+typedef struct ptg_server_config {
+    uint32_t max_slots;           /* concurrent queries on the device; 0 = 256          */
+    uint32_t max_batch;           /* sources per fused batch; 0 = 64                    */
+    uint32_t queue_capacity;      /* pending requests before PTG_ERR_BUSY; 0 = 65536    */
+    uint32_t ppr_iterations;      /* 0 = 20                                             */
+    uint64_t memory_budget_bytes; /* 0 = free HBM at start minus 10%                    */
+} ptg_server_config;
+
+ptg_status ptg_server_create(ptg_ctx *ctx, const ptg_server_config *cfg, ptg_server **out);
+void ptg_server_destroy(ptg_server *s);
+/* Register a graph with the server (the server does not own it). */
+ptg_status ptg_server_add_graph(ptg_server *s, ptg_graph *g, uint32_t *graph_id);
+/* Submit a query; the result buffer (n entries of u32 for BFS/SSSP, float for
+ * PPR, host memory) must stay valid until the request completes. */
+ptg_status ptg_server_submit(ptg_server *s, uint32_t graph_id, uint32_t kind, uint32_t src,
+                             void *result, uint64_t *request_id);
+/* Wait for a request (timeout_ms < 0: forever).  Returns PTG_ERR_TIMEOUT if
+ * not done in time; latency_us receives submit->completion time. */
+ptg_status ptg_server_wait(ptg_server *s, uint64_t request_id, int64_t timeout_ms,
+                           double *latency_us);
+ptg_status ptg_server_drain(ptg_server *s);
+
+typedef struct ptg_server_stats {
+    uint64_t submitted, completed, batches, max_batch_seen;
+    double busy_ms;
+} ptg_server_stats;
+ptg_status ptg_server_stats_get(ptg_server *s, ptg_server_stats *st);
+
+/* ------------------------------------------------------------------------ */
+/* Synthetic inputs (host, multithreaded; no GPU).                          */
+/* ------------------------------------------------------------------------ */
+/* A host CSR allocated by the library (sentinel form, u64 offsets). */
+typedef struct ptg_host_csr {
+    uint64_t n, m;
+    uint64_t *offsets; /* n+1 */
+    uint32_t *col;     /* m   */
+    uint32_t *weight;  /* m or NULL */
+    uint32_t pinned;   /* 1: arrays are pinned (cudaHostAlloc) */
+    uint32_t reserved;
+} ptg_host_csr;
+
+/* RMAT (a, b, c, d = 1-a-b-c) with 2^scale vertices and edge_factor*2^scale
+ * generated edges from a counter-based generator (splitmix64 of seed, edge
+ * index and level), no vertex permutation, self-loops and duplicates
+ * removed, optionally symmetrized.  Weights (wmax > 0) are uniform in
+ * [wmin, wmax] from a hash of (seed, min(u,v), max(u,v)), so both directions
+ * of an edge carry the same weight.  pinned = 1 allocates pinned memory
+ * (needs a CUDA device); 0 uses malloc. */
+ptg_status ptg_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c,
+                        uint64_t seed, int symmetric, uint32_t wmin, uint32_t wmax,
+                        uint32_t threads, int pinned, ptg_host_csr *out);
+/* num_graphs Erdos-Renyi graphs concatenated (vertex ranges vtx_begin[i] ..
+ * vtx_begin[i+1]), vertex counts log-uniform in [nmin, nmax], average degree
+ * avg_degree, symmetric, duplicates and self-loops removed.  vtx_begin is
+ * allocated with num_graphs+1 entries (free with ptg_free). */
+ptg_status ptg_gen_er_batch(uint32_t num_graphs, uint64_t nmin, uint64_t nmax, double avg_degree,
+                            uint64_t seed, uint32_t threads, ptg_host_csr *out,
+                            uint64_t **vtx_begin);
+void ptg_host_csr_free(ptg_host_csr *g);
+void ptg_free(void *p);
+
+/* ------------------------------------------------------------------------ */
+/* Drop-in entry points: the reference's names and parameter lists          */
+/* (ptGraph/main.cu:30-56).  nodePointersI has testNumNodes entries (no     */
+/* sentinel); returns elapsed ms or -1 on error.                            */
+/* ------------------------------------------------------------------------ */
+/* main.cu:1180 - out-of-core BFS (resident prefix + streamed rest). */
+long bfsCaculateInOpt(unsigned int testNumNodes, unsigned int testNumEdge,
+                      unsigned int *nodePointersI, unsigned int *edgeList,
+                      unsigned int sourceNode);
+/* main.cu:1420 - same, static and dynamic parts on separate streams. */
+long bfsCaculateInAsync(unsigned int testNumNodes, unsigned int testNumEdge,
+                        unsigned int *nodePointersI, unsigned int *edgeList,
+                        unsigned int sourceNode);
+/* main.cu:1681 - fragment-aware variant (skips inactive partitions). */
+long bfsCaculateInAsyncSwap(unsigned int testNumNodes, unsigned int testNumEdge,
+                            unsigned int *nodePointersI, unsigned int *edgeList,
+                            unsigned int sourceNode);
+/* main.cu:1041 - the reference's unified-memory BFS; here the whole CSR in HBM. */
+long bfsCaculateInShare(unsigned int testNumNodes, unsigned int testNumEdge,
+                        unsigned int *nodePointersI, unsigned int *edgeList,
+                        unsigned int sourceNode);
+/* main.cu:563 - SSSP, unreached = 0xFFFFFFFE as in the reference. */
+long ssspCaculateInShare(unsigned int testNumNodes, unsigned int testNumEdge,
+                         unsigned int *nodePointersI, ptg_edge_w *edgeList,
+                         unsigned int sourceNode);
+/* main.cu:678 - out-of-core SSSP, unreached = 0xFFFFFFFF. */
+long ssspCaculateInOpt(unsigned int testNumNodes, unsigned int testNumEdge,
+                       unsigned int *nodePointersI, ptg_edge_w *edgeList,
+                       unsigned int sourceNode);
+/* main.cu:961 / main.cu:222 - min-label connected components. */
+long ccCaculateInShare(unsigned int testNumNodes, unsigned int testNumEdge,
+                       unsigned int *nodePointersI, unsigned int *edgeList);
+long ccCaculateInOpt(unsigned int testNumNodes, unsigned int testNumEdge,
+                     unsigned int *nodePointersI, unsigned int *edgeList);
+/* main.cu:891 / main.cu:52 - PageRank (a stub in the reference): 20 pull
+ * iterations, d = 0.85; result in ptg_compat_last_result_f32(). */
+long prCaculateInShare(unsigned int testNumNodes, unsigned int testNumEdge,
+                       unsigned int *nodePointersI, unsigned int *edgeList);
+long prCaculateInOpt(unsigned int testNumNodes, unsigned int testNumEdge,
+                     unsigned int *nodePointersI, unsigned int *edgeList);
+/* main.cu:2396 / main.cu:2061 / main.cu:2196 - BFS variants that take the
+ * source from the reference's own choice (vertex 0 for caculateInCommon; the
+ * first vertex of degree > 1000 for caculateInShareOpt) and return nothing. */
+void caculateInCommon(unsigned int testNumNodes, unsigned int testNumEdge,
+                      unsigned int *nodePointersI, unsigned int *edgeList);
+void caculateInShareOpt(unsigned int testNumNodes, unsigned int testNumEdge,
+                        unsigned int *nodePointersI, unsigned int *edgeList);
+void caculateInOptChooseByDegree(unsigned int testNumNodes, unsigned int testNumEdge,
+                                 unsigned int *nodePointersI, unsigned int *edgeList,
+                                 unsigned int sourceNode);
+
+/* Results and settings of the drop-in entry points (per calling thread). */
+uint64_t ptg_compat_last_result(uint32_t *out, uint64_t capacity);
+uint64_t ptg_compat_last_result_f32(float *out, uint64_t capacity);
+const char *ptg_compat_last_error(void);
+/* Replace the reference's memory fractions / fragment_size for later calls
+ * (NULL restores the defaults). */
+void ptg_compat_set_partition_config(const ptg_partition_config *cfg);
+/* Device the drop-in entry points use (default 0). */
+void ptg_compat_set_device(int device);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PTGRAPH_H */

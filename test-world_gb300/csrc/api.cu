@@ -1,0 +1,744 @@
+// api.cu - C ABI: contexts, graph upload and partition planning, algorithm
+// entry points, and the drop-in entry points with the reference's names.
+//
+// Reference boundary (ptGraph/main.cu:24-56): free C++ functions that take a
+// host CSR, allocate and free all device memory themselves, discard the
+// result and return elapsed ms; errors exit() (gpuAssert, main.cu:15-22).
+// Here a context owns streams and reusable workspace, a graph handle owns the
+// uploaded CSR (or its resident prefix plus a partition schedule), outputs
+// are caller-owned and every failure is a ptg_status.
+#include <unistd.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <thread>
+
+#include "ptg_device.cuh"
+
+using namespace ptg;
+
+namespace ptg {
+
+void set_error(ptg_ctx *ctx, const Error &e) {
+    if (ctx) ctx->last_error = e.msg;
+}
+
+ptg_status guard(ptg_ctx *ctx, const std::function<void()> &fn) {
+    try {
+        fn();
+        return PTG_OK;
+    } catch (const Error &e) {
+        set_error(ctx, e);
+        if (e.status == PTG_ERR_CUDA || e.status == PTG_ERR_OOM) cudaGetLastError();
+        return e.status;
+    } catch (const std::bad_alloc &) {
+        set_error(ctx, Error{PTG_ERR_OOM, "host allocation failed"});
+        return PTG_ERR_OOM;
+    } catch (const std::exception &ex) {
+        set_error(ctx, Error{PTG_ERR_INVALID, ex.what()});
+        return PTG_ERR_INVALID;
+    }
+}
+
+int sm_count_of(ptg_ctx *ctx) { return ctx->sm_count; }
+
+namespace {
+
+// Device-side CSR checks: offsets non-decreasing and within m, targets < n.
+template <class OffT>
+__global__ void k_validate(const OffT *off, uint64_t n, uint64_t m, const uint32_t *col,
+                           uint64_t ncol, unsigned *bad) {
+    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+        if (off[i] > off[i + 1] || (uint64_t)off[i + 1] > m) atomicOr(bad, 1u);
+    }
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < ncol; j += stride) {
+        if (col[j] >= n) atomicOr(bad, 2u);
+    }
+}
+
+__global__ void k_replace_u32(uint32_t *a, uint64_t n, uint32_t from, uint32_t to) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        if (a[i] == from) a[i] = to;
+}
+
+__global__ void k_aos_to_soa(const ptg_edge_w *e, uint64_t m, uint32_t *col, uint32_t *w) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        ptg_edge_w x = e[i];
+        col[i] = x.to;
+        w[i] = x.weight;
+    }
+}
+
+size_t host_page() {
+    long p = sysconf(_SC_PAGESIZE);
+    return p > 0 ? (size_t)p : 4096;
+}
+
+// Normalize offsets to a host u64 sentinel array.
+std::vector<uint64_t> host_offsets(const ptg_csr *c) {
+    std::vector<uint64_t> o(c->n + 1);
+    if (c->offset_type == PTG_OFFSETS_U64) {
+        const uint64_t *src = static_cast<const uint64_t *>(c->offsets);
+        std::memcpy(o.data(), src, c->n * 8);
+        o[c->n] = c->offset_form == PTG_FORM_SENTINEL ? src[c->n] : c->m;
+    } else {
+        const uint32_t *src = static_cast<const uint32_t *>(c->offsets);
+        for (uint64_t i = 0; i < c->n; i++) o[i] = src[i];
+        o[c->n] = c->offset_form == PTG_FORM_SENTINEL ? src[c->n] : c->m;
+    }
+    return o;
+}
+
+void plan(uint64_t n, uint64_t m, const uint64_t *off, uint64_t bpe, const ptg_partition_config *cfg_in,
+          uint64_t device_free, uint64_t &P, uint64_t &R, uint64_t &PE, std::vector<uint64_t> *first) {
+    ptg_partition_config cfg;
+    ptg_partition_config_default(&cfg);
+    if (cfg_in) cfg = *cfg_in;
+    if (cfg.partition_bytes == 0) cfg.partition_bytes = 256ull << 20;
+    if (cfg.n_staging_buffers == 0) cfg.n_staging_buffers = 2;
+    if (cfg.device_frac <= 0) cfg.device_frac = 0.9;
+    PE = std::max<uint64_t>(1, cfg.partition_bytes / bpe);
+    uint64_t budget = cfg.device_budget_bytes ? cfg.device_budget_bytes
+                                              : (uint64_t)(cfg.device_frac * (double)device_free);
+    bool fits = m * bpe <= budget;
+    if (fits && !cfg.force_out_of_core) {
+        P = std::max<uint64_t>(1, (m + PE - 1) / PE);
+        R = P;
+    } else {
+        P = std::max<uint64_t>(1, (m + PE - 1) / PE);
+        uint64_t stage = (uint64_t)cfg.n_staging_buffers * PE * bpe;
+        uint64_t avail = budget > stage ? budget - stage : 0;
+        R = cfg.resident_policy == PTG_RESIDENT_NONE ? 0 : std::min<uint64_t>(P, avail / (PE * bpe));
+        if (R == P && cfg.force_out_of_core) R = P - 1;  // keep at least one streamed partition
+    }
+    if (first) {
+        first->assign(P + 1, 0);
+        for (uint64_t p = 0; p < P; p++) {
+            uint64_t e = p * PE;
+            // owner of edge e: last vertex with off[v] <= e
+            uint64_t v = (uint64_t)(std::upper_bound(off, off + n, e) - off);
+            (*first)[p] = v ? v - 1 : 0;
+        }
+        (*first)[P] = n - 1;
+    }
+}
+
+}  // namespace
+}  // namespace ptg
+
+extern "C" {
+
+const char *ptg_status_string(ptg_status s) {
+    switch (s) {
+        case PTG_OK: return "ok";
+        case PTG_ERR_INVALID: return "invalid argument";
+        case PTG_ERR_OOM: return "out of memory";
+        case PTG_ERR_CUDA: return "CUDA error";
+        case PTG_ERR_TIMEOUT: return "timeout";
+        case PTG_ERR_UNSUPPORTED: return "unsupported";
+        case PTG_ERR_NO_DEVICE: return "no CUDA device";
+        case PTG_ERR_CANCELLED: return "cancelled";
+        case PTG_ERR_BUSY: return "busy";
+    }
+    return "unknown";
+}
+
+void ptg_partition_config_default(ptg_partition_config *cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->partition_bytes = 256ull << 20;
+    cfg->device_budget_bytes = 0;
+    cfg->device_frac = 0.9;
+    cfg->n_staging_buffers = 2;
+    cfg->resident_policy = PTG_RESIDENT_PREFIX;
+    cfg->force_out_of_core = 0;
+    cfg->hot_threshold = 3600;  // gpu_kernels.cu:479
+}
+
+ptg_status ptg_plan_partitions(uint64_t n, uint64_t m, const uint64_t *offsets_n1,
+                               uint64_t bytes_per_edge, const ptg_partition_config *cfg,
+                               uint64_t device_free_bytes, uint64_t *num_partitions,
+                               uint64_t *resident_partitions, uint64_t *partition_edges,
+                               uint64_t *part_first_vertex) {
+    if (!offsets_n1 || n == 0 || bytes_per_edge == 0 || !num_partitions) return PTG_ERR_INVALID;
+    uint64_t P, R, PE;
+    std::vector<uint64_t> first;
+    plan(n, m, offsets_n1, bytes_per_edge, cfg, device_free_bytes, P, R, PE,
+         part_first_vertex ? &first : nullptr);
+    *num_partitions = P;
+    if (resident_partitions) *resident_partitions = R;
+    if (partition_edges) *partition_edges = PE;
+    if (part_first_vertex) std::memcpy(part_first_vertex, first.data(), (P + 1) * 8);
+    return PTG_OK;
+}
+
+ptg_status ptg_ctx_create(int device, ptg_ctx **out) {
+    if (!out) return PTG_ERR_INVALID;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return PTG_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= count) return PTG_ERR_INVALID;
+    auto *ctx = new ptg_ctx();
+    ctx->device = device;
+    ptg_status s = guard(ctx, [&] {
+        PTG_CUDA_TRY(cudaSetDevice(device));
+        cudaDeviceProp prop;
+        PTG_CUDA_TRY(cudaGetDeviceProperties(&prop, device));
+        ctx->sm_count = prop.multiProcessorCount;
+        ctx->hbm_bytes = prop.totalGlobalMem;
+        PTG_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        PTG_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
+        PTG_CUDA_TRY(cudaEventCreate(&ctx->ev0));
+        PTG_CUDA_TRY(cudaEventCreate(&ctx->ev1));
+    });
+    if (s != PTG_OK) {
+        ptg_ctx_destroy(ctx);
+        return s;
+    }
+    *out = ctx;
+    return PTG_OK;
+}
+
+void ptg_ctx_destroy(ptg_ctx *ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    delete ctx;
+}
+
+const char *ptg_ctx_last_error(const ptg_ctx *ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+ptg_status ptg_ctx_profile_enable(ptg_ctx *ctx, int enable) {
+    if (!ctx) return PTG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ctx->prof.reset();
+    ctx->prof.enabled = enable != 0;
+    return PTG_OK;
+}
+
+uint64_t ptg_ctx_launch_count(const ptg_ctx *ctx) { return ctx ? ctx->prof.launches : 0; }
+
+uint32_t ptg_ctx_profile_entries(const ptg_ctx *ctx) {
+    return ctx ? (uint32_t)ctx->prof.names.size() : 0;
+}
+
+ptg_status ptg_ctx_profile_entry(const ptg_ctx *ctx, uint32_t i, const char **name,
+                                 uint64_t *launches, double *total_ms) {
+    if (!ctx || i >= ctx->prof.names.size()) return PTG_ERR_INVALID;
+    if (name) *name = ctx->prof.names[i].c_str();
+    if (launches) *launches = ctx->prof.counts[i];
+    if (total_ms) *total_ms = ctx->prof.ms[i];
+    return PTG_OK;
+}
+
+ptg_status ptg_ctx_device_info(const ptg_ctx *ctx, int *sm_count, uint64_t *hbm_bytes,
+                               uint64_t *free_bytes) {
+    if (!ctx) return PTG_ERR_INVALID;
+    if (sm_count) *sm_count = ctx->sm_count;
+    if (hbm_bytes) *hbm_bytes = ctx->hbm_bytes;
+    if (free_bytes) {
+        size_t f = 0, t = 0;
+        cudaSetDevice(ctx->device);
+        if (cudaMemGetInfo(&f, &t) != cudaSuccess) return PTG_ERR_CUDA;
+        *free_bytes = f;
+    }
+    return PTG_OK;
+}
+
+void ptg_graph_destroy(ptg_graph *g) {
+    if (!g) return;
+    cudaSetDevice(g->ctx->device);
+    cudaStreamSynchronize(g->ctx->stream);
+    cudaStreamSynchronize(g->ctx->copy_stream);
+    for (void *p : g->registered) cudaHostUnregister(p);
+    for (int i = 0; i < 3; i++) {
+        if (g->stage_ready[i]) cudaEventDestroy(g->stage_ready[i]);
+        if (g->stage_free[i]) cudaEventDestroy(g->stage_free[i]);
+    }
+    delete g;
+}
+
+ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partition_config *cfg_in,
+                            ptg_graph **out) {
+    if (!ctx || !csr || !out) return PTG_ERR_INVALID;
+    *out = nullptr;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto *g = new ptg_graph();
+    g->ctx = ctx;
+    ptg_status s = guard(ctx, [&] {
+        PTG_REQUIRE(csr->n >= 1, PTG_ERR_INVALID, "graph needs at least one vertex");
+        PTG_REQUIRE(csr->n < 0xFFFFFFFFull, PTG_ERR_INVALID, "vertex ids are 32-bit: n must be < 2^32-1");
+        PTG_REQUIRE(csr->offsets != nullptr, PTG_ERR_INVALID, "offsets is NULL");
+        PTG_REQUIRE(csr->m == 0 || csr->col || csr->edges_aos, PTG_ERR_INVALID, "edge array is NULL");
+        PTG_REQUIRE(csr->offset_type == PTG_OFFSETS_U64 || csr->m < (1ull << 32), PTG_ERR_INVALID,
+                    "u32 offsets cannot address m >= 2^32 edges");
+        PTG_CUDA_TRY(cudaSetDevice(ctx->device));
+        cudaStream_t st = ctx->stream;
+        g->n = csr->n;
+        g->m = csr->m;
+        g->symmetric = (csr->flags & PTG_CSR_SYMMETRIC) != 0;
+        g->weighted = csr->weight != nullptr || csr->edges_aos != nullptr;
+        g->off64 = csr->m >= (1ull << 32);
+        std::vector<uint64_t> off = host_offsets(csr);
+        PTG_REQUIRE(off[0] == 0 && off[g->n] == g->m, PTG_ERR_INVALID,
+                    "offsets must start at 0 and end at m");
+        ptg_partition_config cfg;
+        ptg_partition_config_default(&cfg);
+        if (cfg_in) cfg = *cfg_in;
+        if (cfg.n_staging_buffers < 2) cfg.n_staging_buffers = 2;
+        if (cfg.n_staging_buffers > 3) cfg.n_staging_buffers = 3;
+        uint64_t bpe = g->weighted ? 8 : 4;
+        size_t dfree = 0, dtot = 0;
+        PTG_CUDA_TRY(cudaMemGetInfo(&dfree, &dtot));
+        // keep room for the traversal workspace (~40 bytes per vertex, the
+        // reference's own reserve is 10 * 4 * n, main.cu:1193)
+        uint64_t reserve = 48ull * g->n + (512ull << 20);
+        uint64_t usable = dfree > reserve ? dfree - reserve : 0;
+        uint64_t P, R, PE;
+        plan(g->n, g->m, off.data(), bpe, &cfg, usable, P, R, PE, &g->part_first_vertex);
+        g->num_partitions = P;
+        g->resident_partitions = R;
+        g->partition_edges = PE;
+        g->resident_edges = std::min<uint64_t>(g->m, R * PE);
+        g->out_of_core = g->resident_edges < g->m;
+        g->n_stage = cfg.n_staging_buffers;
+        g->resident_policy = cfg.resident_policy;
+        g->hot_threshold = cfg.hot_threshold;
+
+        // offsets
+        size_t osz = g->off64 ? 8 : 4;
+        g->d_off.ensure((g->n + 1) * osz);
+        if (g->off64) {
+            PTG_CUDA_TRY(cudaMemcpyAsync(g->d_off.p, off.data(), (g->n + 1) * 8, cudaMemcpyHostToDevice, st));
+            PTG_CUDA_TRY(cudaStreamSynchronize(st));
+        } else {
+            std::vector<uint32_t> o32(g->n + 1);
+            for (uint64_t i = 0; i <= g->n; i++) o32[i] = (uint32_t)off[i];
+            PTG_CUDA_TRY(cudaMemcpyAsync(g->d_off.p, o32.data(), (g->n + 1) * 4, cudaMemcpyHostToDevice, st));
+            PTG_CUDA_TRY(cudaStreamSynchronize(st));
+        }
+        g->device_bytes = (g->n + 1) * osz;
+
+        // resident edges (SoA in HBM)
+        uint64_t RE = g->resident_edges;
+        g->d_col.ensure(std::max<uint64_t>(RE, 1) * 4);
+        if (g->weighted) g->d_w.ensure(std::max<uint64_t>(RE, 1) * 4);
+        if (RE) {
+            if (csr->col) {
+                PTG_CUDA_TRY(cudaMemcpyAsync(g->d_col.p, csr->col, RE * 4, cudaMemcpyHostToDevice, st));
+                if (csr->weight)
+                    PTG_CUDA_TRY(cudaMemcpyAsync(g->d_w.p, csr->weight, RE * 4, cudaMemcpyHostToDevice, st));
+            } else {
+                // reference AoS records: stage through HBM in chunks and split
+                DevBuf tmp;
+                uint64_t chunk = std::min<uint64_t>(RE, 1ull << 26);
+                tmp.ensure(chunk * 8);
+                for (uint64_t e = 0; e < RE; e += chunk) {
+                    uint64_t c = std::min<uint64_t>(chunk, RE - e);
+                    PTG_CUDA_TRY(cudaMemcpyAsync(tmp.p, csr->edges_aos + e, c * 8, cudaMemcpyHostToDevice, st));
+                    launch(ctx, "k_aos_to_soa", k_aos_to_soa, grid_for(c, kBlock, ctx->sm_count * 8), kBlock, 0,
+                           st, tmp.as<ptg_edge_w>(), c, g->d_col.as<uint32_t>() + e, g->d_w.as<uint32_t>() + e);
+                    PTG_CUDA_TRY(cudaStreamSynchronize(st));
+                }
+            }
+        }
+        g->device_bytes += RE * bpe;
+
+        // validate on the device
+        DevBuf bad;
+        bad.ensure(4);
+        PTG_CUDA_TRY(cudaMemsetAsync(bad.p, 0, 4, st));
+        if (g->off64)
+            launch(ctx, "k_validate", k_validate<unsigned long long>, ctx->sm_count * 8, kBlock, 0, st,
+                   g->d_off.as<unsigned long long>(), g->n, g->m, g->d_col.as<uint32_t>(), RE, bad.as<unsigned>());
+        else
+            launch(ctx, "k_validate", k_validate<uint32_t>, ctx->sm_count * 8, kBlock, 0, st,
+                   g->d_off.as<uint32_t>(), g->n, g->m, g->d_col.as<uint32_t>(), RE, bad.as<unsigned>());
+        unsigned hbad = 0;
+        PTG_CUDA_TRY(cudaMemcpyAsync(&hbad, bad.p, 4, cudaMemcpyDeviceToHost, st));
+        PTG_CUDA_TRY(cudaStreamSynchronize(st));
+        PTG_REQUIRE(!(hbad & 1), PTG_ERR_INVALID, "offsets are not non-decreasing within [0, m]");
+        PTG_REQUIRE(!(hbad & 2), PTG_ERR_INVALID, "an edge target is >= n");
+
+        if (g->out_of_core) {
+            // host side of the streamed partitions: pinned SoA arrays
+            uint64_t e0 = RE, ne = g->m - RE;
+            const uint32_t *hc = csr->col, *hw = csr->weight;
+            bool own = csr->col == nullptr;  // AoS input: build owned pinned SoA copies
+            if (!own) {
+                for (uint64_t j = e0; j < g->m; j++)
+                    PTG_REQUIRE(hc[j] < g->n, PTG_ERR_INVALID, "an edge target is >= n");
+            }
+            if (own) {
+                g->own_col.ensure(g->m * 4);
+                g->own_w.ensure(g->m * 4);
+                for (uint64_t j = 0; j < g->m; j++) {
+                    PTG_REQUIRE(csr->edges_aos[j].to < g->n, PTG_ERR_INVALID, "an edge target is >= n");
+                    g->own_col.as<uint32_t>()[j] = csr->edges_aos[j].to;
+                    g->own_w.as<uint32_t>()[j] = csr->edges_aos[j].weight;
+                }
+                g->h_col = g->own_col.as<uint32_t>();
+                g->h_w = g->own_w.as<uint32_t>();
+            } else if (csr->flags & PTG_CSR_HOST_PINNED) {
+                g->h_col = hc;
+                g->h_w = hw;
+            } else {
+                // register the caller's streamed range (page-aligned)
+                size_t pg = host_page();
+                auto reg = [&](const uint32_t *base, PinnedBuf &fallback, const uint32_t *&dst) {
+                    uintptr_t a = (uintptr_t)(base + e0), b = (uintptr_t)(base + g->m);
+                    uintptr_t a0 = a & ~(uintptr_t)(pg - 1), b1 = (b + pg - 1) & ~(uintptr_t)(pg - 1);
+                    cudaError_t e = cudaHostRegister((void *)a0, b1 - a0, cudaHostRegisterDefault);
+                    if (e == cudaSuccess) {
+                        g->registered.push_back((void *)a0);
+                        dst = base;
+                    } else {
+                        cudaGetLastError();
+                        fallback.ensure(g->m * 4);
+                        std::memcpy(fallback.as<uint32_t>() + e0, base + e0, ne * 4);
+                        dst = fallback.as<uint32_t>();
+                    }
+                };
+                reg(hc, g->own_col, g->h_col);
+                if (hw) reg(hw, g->own_w, g->h_w);
+            }
+            for (uint32_t b = 0; b < g->n_stage; b++) {
+                g->stage_col[b].ensure(PE * 4);
+                if (g->weighted) g->stage_w[b].ensure(PE * 4);
+                PTG_CUDA_TRY(cudaEventCreateWithFlags(&g->stage_ready[b], cudaEventDisableTiming));
+                PTG_CUDA_TRY(cudaEventCreateWithFlags(&g->stage_free[b], cudaEventDisableTiming));
+            }
+            g->device_bytes += (uint64_t)g->n_stage * PE * bpe;
+            g->part_visits.assign(P, 0);
+        }
+    });
+    if (s != PTG_OK) {
+        ptg_graph_destroy(g);
+        return s;
+    }
+    *out = g;
+    return PTG_OK;
+}
+
+ptg_status ptg_graph_info_get(const ptg_graph *g, ptg_graph_info *info) {
+    if (!g || !info) return PTG_ERR_INVALID;
+    info->n = g->n;
+    info->m = g->m;
+    info->symmetric = g->symmetric;
+    info->weighted = g->weighted;
+    info->out_of_core = g->out_of_core;
+    info->offsets_u64 = g->off64;
+    info->partitions = g->num_partitions;
+    info->resident_partitions = g->resident_partitions;
+    info->partition_edges = g->partition_edges;
+    info->resident_edges = g->resident_edges;
+    info->device_bytes = g->device_bytes;
+    return PTG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// algorithm entry points
+// ---------------------------------------------------------------------------
+namespace {
+
+void fill_stats(ptg_run_stats *st, const RunResult &rr) {
+    if (!st) return;
+    st->iterations = rr.iterations;
+    st->bottom_up_rounds = rr.bottom_up_rounds;
+    st->edges_relaxed = rr.edges_relaxed;
+    st->link_bytes = rr.link_bytes;
+    st->partitions_streamed = rr.parts_streamed;
+    st->partitions_skipped = rr.parts_skipped;
+    st->device_ms = rr.device_ms;
+    st->link_ms = rr.link_ms;
+}
+
+// Run `body` on the context stream with the output in device memory, timing
+// it with events; copy to the host afterwards unless the caller's pointer is
+// already device memory.
+template <class T>
+ptg_status run_u32(ptg_graph *g, T *out, uint32_t flags, ptg_run_stats *stats,
+                   const std::function<void(T *, RunResult &)> &body) {
+    if (!g || !out) return PTG_ERR_INVALID;
+    ptg_ctx *ctx = g->ctx;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return guard(ctx, [&] {
+        PTG_CUDA_TRY(cudaSetDevice(ctx->device));
+        cudaStream_t st = ctx->stream;
+        T *d_out = out;
+        if (!(flags & PTG_OUT_DEVICE)) {
+            ctx->ws.value.ensure(g->n * sizeof(T));
+            d_out = ctx->ws.value.as<T>();
+        }
+        RunResult rr;
+        PTG_CUDA_TRY(cudaEventRecord(ctx->ev0, st));
+        body(d_out, rr);
+        PTG_CUDA_TRY(cudaEventRecord(ctx->ev1, st));
+        if (!(flags & PTG_OUT_DEVICE))
+            PTG_CUDA_TRY(cudaMemcpyAsync(out, d_out, g->n * sizeof(T), cudaMemcpyDeviceToHost, st));
+        PTG_CUDA_TRY(cudaStreamSynchronize(st));
+        ctx->prof.resolve();
+        float ms = 0;
+        PTG_CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+        rr.device_ms = ms;
+        fill_stats(stats, rr);
+        if (stats) {
+            stats->vertices_reached = 0;
+            stats->edges_in_component = 0;
+        }
+    });
+}
+
+void post_unreached(ptg_graph *g, uint32_t *d_out, uint32_t flags) {
+    if (flags & PTG_UNREACHED_MINUS1) {
+        launch(g->ctx, "k_replace_u32", k_replace_u32, grid_for(g->n, kBlock, g->ctx->sm_count * 8), kBlock, 0,
+               g->ctx->stream, d_out, g->n, PTG_UNREACHED, PTG_UNREACHED - 1);
+        PTG_CUDA_TRY(cudaGetLastError());
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+ptg_status ptg_bfs(ptg_graph *g, uint32_t src, uint32_t *levels, const ptg_run_opts *opts) {
+    if (!g || src >= g->n) return PTG_ERR_INVALID;
+    uint32_t flags = opts ? opts->flags : 0;
+    return run_u32<uint32_t>(g, levels, flags, opts ? opts->stats : nullptr, [&](uint32_t *d, RunResult &rr) {
+        run_traversal(g, TRAV_BFS, src, d, flags, 0, opts ? opts->max_iterations : 0, rr);
+        post_unreached(g, d, flags);
+    });
+}
+
+ptg_status ptg_sssp(ptg_graph *g, uint32_t src, uint32_t *dist, const ptg_run_opts *opts) {
+    if (!g || src >= g->n) return PTG_ERR_INVALID;
+    if (!g->weighted) {
+        g->ctx->last_error = "SSSP needs edge weights";
+        return PTG_ERR_INVALID;
+    }
+    uint32_t flags = opts ? opts->flags : 0;
+    return run_u32<uint32_t>(g, dist, flags, opts ? opts->stats : nullptr, [&](uint32_t *d, RunResult &rr) {
+        run_traversal(g, TRAV_SSSP, src, d, flags, opts ? opts->delta : 0, opts ? opts->max_iterations : 0, rr);
+        post_unreached(g, d, flags);
+    });
+}
+
+ptg_status ptg_cc(ptg_graph *g, uint32_t *labels, const ptg_run_opts *opts) {
+    if (!g) return PTG_ERR_INVALID;
+    uint32_t flags = opts ? opts->flags : 0;
+    return run_u32<uint32_t>(g, labels, flags, opts ? opts->stats : nullptr, [&](uint32_t *d, RunResult &rr) {
+        if (g->symmetric && !(flags & PTG_REFERENCE_SCHEDULE)) run_cc_hook(g, d, rr);
+        else run_traversal(g, TRAV_CCPROP, 0, d, flags, 0, opts ? opts->max_iterations : 0, rr);
+    });
+}
+
+static ptg_status pr_common(ptg_graph *g, bool personalized, uint32_t src, float *rank,
+                            const ptg_pr_opts *opts) {
+    if (!g || (personalized && src >= g->n)) return PTG_ERR_INVALID;
+    uint32_t flags = opts ? opts->flags : 0;
+    uint32_t iters = opts && opts->iterations ? opts->iterations : 20;
+    double d = opts && opts->damping > 0 ? opts->damping : 0.85;
+    return run_u32<float>(g, rank, flags, opts ? opts->stats : nullptr, [&](float *dr, RunResult &rr) {
+        run_pagerank(g, personalized, src, d, iters, dr, rr);
+    });
+}
+
+ptg_status ptg_pagerank(ptg_graph *g, float *rank, const ptg_pr_opts *opts) {
+    return pr_common(g, false, 0, rank, opts);
+}
+
+ptg_status ptg_ppr(ptg_graph *g, uint32_t src, float *rank, const ptg_pr_opts *opts) {
+    return pr_common(g, true, src, rank, opts);
+}
+
+ptg_status ptg_cc_batch(ptg_ctx *ctx, uint32_t num_graphs, const uint64_t *vtx_begin,
+                        const uint64_t *offsets, const uint32_t *col, uint32_t *labels,
+                        const ptg_run_opts *opts) {
+    if (!ctx || !vtx_begin || !offsets || !labels || num_graphs == 0) return PTG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    return guard(ctx, [&] {
+        PTG_CUDA_TRY(cudaSetDevice(ctx->device));
+        RunResult rr;
+        run_cc_batch(ctx, num_graphs, vtx_begin, offsets, col, labels, rr);
+        ctx->prof.resolve();
+        if (opts) fill_stats(opts->stats, rr);
+    });
+}
+
+// ---------------------------------------------------------------------------
+// drop-in entry points (ptGraph/main.cu:24-56)
+// ---------------------------------------------------------------------------
+namespace {
+struct CompatState {
+    int device = 0;
+    bool have_cfg = false;
+    ptg_partition_config cfg;
+    std::vector<uint32_t> last;
+    std::vector<float> last_f;
+    std::string err;
+    ptg_ctx *ctx = nullptr;
+    int ctx_device = -1;
+    ~CompatState() {
+        if (ctx) ptg_ctx_destroy(ctx);
+    }
+};
+thread_local CompatState tls;
+
+ptg_ctx *compat_ctx() {
+    if (tls.ctx && tls.ctx_device == tls.device) return tls.ctx;
+    if (tls.ctx) ptg_ctx_destroy(tls.ctx);
+    tls.ctx = nullptr;
+    ptg_status s = ptg_ctx_create(tls.device, &tls.ctx);
+    if (s != PTG_OK) {
+        tls.err = std::string("context: ") + ptg_status_string(s);
+        return nullptr;
+    }
+    tls.ctx_device = tls.device;
+    return tls.ctx;
+}
+
+// kind: 0 bfs, 1 sssp, 2 cc, 3 pr.  frac: the reference's memory fraction
+// for this entry point (used unless a partition config was set).
+long compat_run(int kind, unsigned n, unsigned m, unsigned *off_n, const unsigned *col,
+                const ptg_edge_w *aos, unsigned src, double frac, uint32_t flags, bool symmetric) {
+    auto t0 = std::chrono::steady_clock::now();
+    tls.err.clear();
+    ptg_ctx *ctx = compat_ctx();
+    if (!ctx) return -1;
+    if (n == 0 || !off_n || (m && !col && !aos)) {
+        tls.err = "invalid CSR";
+        return -1;
+    }
+    ptg_csr c{};
+    c.n = n;
+    c.m = m;
+    c.offsets = off_n;
+    c.offset_type = PTG_OFFSETS_U32;
+    c.offset_form = PTG_FORM_REFERENCE;
+    c.col = col;
+    c.edges_aos = aos;
+    c.flags = symmetric ? PTG_CSR_SYMMETRIC : 0;
+    ptg_partition_config cfg;
+    ptg_partition_config_default(&cfg);
+    cfg.device_frac = frac;
+    if (tls.have_cfg) cfg = tls.cfg;
+    ptg_graph *g = nullptr;
+    ptg_status s = ptg_graph_create(ctx, &c, &cfg, &g);
+    if (s != PTG_OK) {
+        tls.err = ptg_ctx_last_error(ctx);
+        return -1;
+    }
+    ptg_run_stats stats{};
+    ptg_run_opts o{};
+    o.flags = flags;
+    o.stats = &stats;
+    if (kind == 3) {
+        tls.last_f.resize(n);
+        ptg_pr_opts po{};
+        po.stats = &stats;
+        s = ptg_pagerank(g, tls.last_f.data(), &po);
+    } else {
+        tls.last.resize(n);
+        if (kind == 0) s = ptg_bfs(g, src, tls.last.data(), &o);
+        else if (kind == 1) s = ptg_sssp(g, src, tls.last.data(), &o);
+        else s = ptg_cc(g, tls.last.data(), &o);
+    }
+    if (s != PTG_OK) tls.err = ptg_ctx_last_error(ctx);
+    ptg_graph_destroy(g);
+    if (s != PTG_OK) return -1;
+    auto t1 = std::chrono::steady_clock::now();
+    (void)t0;
+    (void)t1;
+    return (long)(stats.device_ms + 0.5);
+}
+}  // namespace
+
+long bfsCaculateInOpt(unsigned n, unsigned m, unsigned *off, unsigned *col, unsigned src) {
+    return compat_run(0, n, m, off, col, nullptr, src, 0.8, 0, false);  // main.cu:1193
+}
+long bfsCaculateInAsync(unsigned n, unsigned m, unsigned *off, unsigned *col, unsigned src) {
+    return compat_run(0, n, m, off, col, nullptr, src, 0.6, 0, false);  // main.cu:1433
+}
+long bfsCaculateInAsyncSwap(unsigned n, unsigned m, unsigned *off, unsigned *col, unsigned src) {
+    return compat_run(0, n, m, off, col, nullptr, src, 0.6, 0, false);  // main.cu:1693
+}
+long bfsCaculateInShare(unsigned n, unsigned m, unsigned *off, unsigned *col, unsigned src) {
+    return compat_run(0, n, m, off, col, nullptr, src, 0.9, 0, false);
+}
+long ssspCaculateInShare(unsigned n, unsigned m, unsigned *off, ptg_edge_w *edges, unsigned src) {
+    return compat_run(1, n, m, off, nullptr, edges, src, 0.9, PTG_UNREACHED_MINUS1, false);
+}
+long ssspCaculateInOpt(unsigned n, unsigned m, unsigned *off, ptg_edge_w *edges, unsigned src) {
+    return compat_run(1, n, m, off, nullptr, edges, src, 0.5, 0, false);  // main.cu:694
+}
+long ccCaculateInShare(unsigned n, unsigned m, unsigned *off, unsigned *col) {
+    return compat_run(2, n, m, off, col, nullptr, 0, 0.9, 0, false);
+}
+long ccCaculateInOpt(unsigned n, unsigned m, unsigned *off, unsigned *col) {
+    return compat_run(2, n, m, off, col, nullptr, 0, 0.7, 0, false);  // main.cu:237
+}
+long prCaculateInShare(unsigned n, unsigned m, unsigned *off, unsigned *col) {
+    return compat_run(3, n, m, off, col, nullptr, 0, 0.9, 0, true);
+}
+long prCaculateInOpt(unsigned n, unsigned m, unsigned *off, unsigned *col) {
+    return compat_run(3, n, m, off, col, nullptr, 0, 0.9, 0, true);
+}
+void caculateInCommon(unsigned n, unsigned m, unsigned *off, unsigned *col) {
+    compat_run(0, n, m, off, col, nullptr, 0, 0.9, 0, false);  // source 0, main.cu:2418
+}
+void caculateInShareOpt(unsigned n, unsigned m, unsigned *off, unsigned *col) {
+    // source: first vertex with degree > 1000 (main.cu:2103-2109), else 0
+    unsigned src = 0;
+    for (unsigned i = 0; off && i + 1 < n; i++) {
+        if (off[i + 1] - off[i] > 1000) {
+            src = i;
+            break;
+        }
+    }
+    compat_run(0, n, m, off, col, nullptr, src, 0.9, 0, false);
+}
+void caculateInOptChooseByDegree(unsigned n, unsigned m, unsigned *off, unsigned *col, unsigned src) {
+    compat_run(0, n, m, off, col, nullptr, src, 0.9, 0, false);
+}
+
+uint64_t ptg_compat_last_result(uint32_t *out, uint64_t capacity) {
+    uint64_t k = std::min<uint64_t>(capacity, tls.last.size());
+    if (out && k) std::memcpy(out, tls.last.data(), k * 4);
+    return tls.last.size();
+}
+uint64_t ptg_compat_last_result_f32(float *out, uint64_t capacity) {
+    uint64_t k = std::min<uint64_t>(capacity, tls.last_f.size());
+    if (out && k) std::memcpy(out, tls.last_f.data(), k * 4);
+    return tls.last_f.size();
+}
+const char *ptg_compat_last_error(void) { return tls.err.c_str(); }
+void ptg_compat_set_partition_config(const ptg_partition_config *cfg) {
+    if (cfg) {
+        tls.cfg = *cfg;
+        tls.have_cfg = true;
+    } else {
+        tls.have_cfg = false;
+    }
+}
+void ptg_compat_set_device(int device) { tls.device = device; }
+
+}  // extern "C"

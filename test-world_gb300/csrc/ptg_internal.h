@@ -1,0 +1,283 @@
+// ptg_internal.h - internal types of the GB300 graph engine (host + device).
+//
+// Layout in HBM (one ptg_graph):
+//   offsets   : OffT[n+1]   (u32 when m < 2^32, else u64; sentinel form)
+//   col       : u32[resident_edges]      (structure of arrays)
+//   weight    : u32[resident_edges]      (weighted graphs only)
+// Edges past resident_edges stay in (pinned) host memory and stream through
+// n_staging_buffers device buffers of partition_edges edges each.
+//
+// Per-query working state (ptg_workspace) is owned by the context and reused:
+//   value u32[n], two frontier queues u32[n], two frontier bitmaps, the scan
+//   arrays of the load-balanced expand, the far pile of near/far SSSP, and a
+//   small control block (TravCtl) that kernels read their sizes from, so no
+//   kernel needs a host round trip to learn how much work it has.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <functional>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/ptgraph.h"
+
+#define PTG_UNREACHED 0xFFFFFFFFu
+
+namespace ptg {
+
+// --------------------------------------------------------------------------
+// errors
+// --------------------------------------------------------------------------
+struct Error {
+    ptg_status status;
+    std::string msg;
+};
+
+#define PTG_CUDA_TRY(expr)                                                              \
+    do {                                                                                \
+        cudaError_t _e = (expr);                                                        \
+        if (_e != cudaSuccess) {                                                        \
+            throw ::ptg::Error{_e == cudaErrorMemoryAllocation ? PTG_ERR_OOM : PTG_ERR_CUDA, \
+                               std::string(#expr) + ": " + cudaGetErrorString(_e) + " (" + \
+                                   __FILE__ + ":" + std::to_string(__LINE__) + ")"};    \
+        }                                                                               \
+    } while (0)
+
+#define PTG_REQUIRE(cond, status, text)                                                 \
+    do {                                                                                \
+        if (!(cond)) throw ::ptg::Error{status, text};                                  \
+    } while (0)
+
+// --------------------------------------------------------------------------
+// device buffer (RAII)
+// --------------------------------------------------------------------------
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    // grow-only reallocation
+    void ensure(size_t want) {
+        if (want <= bytes && p) return;
+        release();
+        size_t b = want ? want : 16;
+        PTG_CUDA_TRY(cudaMalloc(&p, b));
+        bytes = b;
+    }
+    template <class T>
+    T *as() const {
+        return reinterpret_cast<T *>(p);
+    }
+};
+
+struct PinnedBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf &) = delete;
+    PinnedBuf &operator=(const PinnedBuf &) = delete;
+    ~PinnedBuf() { release(); }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void ensure(size_t want) {
+        if (want <= bytes && p) return;
+        release();
+        size_t b = want ? want : 16;
+        PTG_CUDA_TRY(cudaHostAlloc(&p, b, cudaHostAllocDefault));
+        bytes = b;
+    }
+    template <class T>
+    T *as() const {
+        return reinterpret_cast<T *>(p);
+    }
+};
+
+// --------------------------------------------------------------------------
+// control block read by the traversal kernels (device memory)
+// --------------------------------------------------------------------------
+struct TravCtl {
+    unsigned long long E;         // edges of the current frontier (scan total)
+    unsigned long long edges_done;// running total of edges expanded (stats)
+    unsigned long long m_unvisited; // BFS direction heuristic
+    unsigned long long far_min;   // min dist over the far pile (near/far SSSP)
+    unsigned int F;               // current frontier size
+    unsigned int next_tail;       // next frontier append cursor
+    unsigned int far_count;       // far pile size
+    unsigned int far_tail;        // far pile append cursor (split output)
+    unsigned int threshold;       // near/far split value (SSSP)
+    unsigned int dir;             // 0 top-down, 1 bottom-up
+    unsigned int level_val;       // BFS: value of current frontier vertices
+    unsigned int error;           // nonzero: a kernel detected a bad index
+    unsigned int pad[4];
+};
+
+// --------------------------------------------------------------------------
+// kernel profiler: counts every launch; when enabled, brackets each launch
+// with CUDA events on its own stream and accumulates per-kernel device time.
+// --------------------------------------------------------------------------
+struct Prof {
+    bool enabled = false;
+    uint64_t launches = 0;
+    struct Rec {
+        const char *name;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::string> names;
+    std::vector<uint64_t> counts;
+    std::vector<double> ms;
+    Rec cur{};
+    cudaEvent_t get() {
+        if (!pool.empty()) {
+            cudaEvent_t e = pool.back();
+            pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e = nullptr;
+        cudaEventCreate(&e);
+        return e;
+    }
+    void begin(const char *name, cudaStream_t st) {
+        launches++;
+        if (!enabled) return;
+        cur = Rec{name, get(), get()};
+        cudaEventRecord(cur.a, st);
+    }
+    void end(cudaStream_t st) {
+        if (!enabled) return;
+        cudaEventRecord(cur.b, st);
+        pending.push_back(cur);
+    }
+    // fold finished records into the totals (call after a synchronize)
+    void resolve() {
+        for (auto &r : pending) {
+            cudaEventSynchronize(r.b);
+            float t = 0;
+            cudaEventElapsedTime(&t, r.a, r.b);
+            size_t i = 0;
+            while (i < names.size() && names[i] != r.name) i++;
+            if (i == names.size()) {
+                names.emplace_back(r.name);
+                counts.push_back(0);
+                ms.push_back(0);
+            }
+            counts[i]++;
+            ms[i] += t;
+            pool.push_back(r.a);
+            pool.push_back(r.b);
+        }
+        pending.clear();
+    }
+    void reset() {
+        resolve();
+        names.clear();
+        counts.clear();
+        ms.clear();
+    }
+    ~Prof() {
+        for (auto &r : pending) {
+            cudaEventDestroy(r.a);
+            cudaEventDestroy(r.b);
+        }
+        for (auto e : pool) cudaEventDestroy(e);
+    }
+};
+
+// --------------------------------------------------------------------------
+// context / graph
+// --------------------------------------------------------------------------
+struct Workspace {
+    DevBuf value, q[2], bm[2], farq[2], farbm, scan, rowstart, bsum, ctl, aux, aux2, flags;
+    PinnedBuf h_ctl, h_flags;
+};
+
+struct Graph;
+
+}  // namespace ptg
+
+struct ptg_ctx {
+    int device = 0;
+    int sm_count = 0;
+    uint64_t hbm_bytes = 0;
+    cudaStream_t stream = nullptr;       // compute stream
+    cudaStream_t copy_stream = nullptr;  // host->device partition stream
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    std::mutex mu;                       // one query at a time per context
+    std::string last_error;
+    ptg::Prof prof;
+    ptg::Workspace ws;
+};
+
+struct ptg_graph {
+    ptg_ctx *ctx = nullptr;
+    uint64_t n = 0, m = 0;
+    bool symmetric = false, weighted = false, off64 = false;
+    // device copies
+    ptg::DevBuf d_off, d_col, d_w, d_invdeg;
+    // out-of-core
+    bool out_of_core = false;
+    uint64_t resident_edges = 0;
+    uint64_t partition_edges = 0;
+    uint64_t num_partitions = 0, resident_partitions = 0;
+    std::vector<uint64_t> part_first_vertex;  // [P+1]
+    ptg::DevBuf d_part_first_vertex;
+    const uint32_t *h_col = nullptr, *h_w = nullptr;  // pinned host edge arrays
+    std::vector<void *> registered;                    // cudaHostRegister'ed ranges
+    ptg::PinnedBuf own_col, own_w;                     // owned pinned copies
+    ptg::DevBuf stage_col[3], stage_w[3];
+    uint32_t n_stage = 2;
+    cudaEvent_t stage_ready[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t stage_free[3] = {nullptr, nullptr, nullptr};
+    uint64_t device_bytes = 0;
+    // hot-partition residency
+    uint32_t resident_policy = PTG_RESIDENT_PREFIX;
+    uint32_t hot_threshold = 3600;
+    std::vector<uint64_t> part_visits;
+};
+
+namespace ptg {
+
+// launch geometry
+constexpr int kBlock = 256;
+constexpr int kItems = 8;
+constexpr int kTile = kBlock * kItems;  // edges per expand tile
+
+void set_error(ptg_ctx *ctx, const Error &e);
+ptg_status guard(ptg_ctx *ctx, const std::function<void()> &fn);
+
+// kernel-side entry points (defined in the .cu files)
+struct RunResult {
+    uint32_t iterations = 0, bottom_up_rounds = 0;
+    uint64_t edges_relaxed = 0, link_bytes = 0, parts_streamed = 0, parts_skipped = 0;
+    double device_ms = 0, link_ms = 0;
+};
+
+enum TravKind { TRAV_BFS = 0, TRAV_SSSP = 1, TRAV_CCPROP = 2 };
+
+void run_traversal(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value, uint32_t flags,
+                   uint32_t delta, uint32_t max_iters, RunResult &rr);
+void run_cc_hook(ptg_graph *g, uint32_t *d_label, RunResult &rr);
+void run_pagerank(ptg_graph *g, bool personalized, uint32_t src, double damping, uint32_t iters,
+                  float *d_rank, RunResult &rr);
+void run_msbfs(ptg_graph *g, const uint32_t *sources, uint32_t k, uint32_t *out, bool out_device,
+               bool weighted, RunResult &rr);
+void run_cc_batch(ptg_ctx *ctx, uint32_t num_graphs, const uint64_t *vtx_begin,
+                  const uint64_t *offsets, const uint32_t *col, uint32_t *labels, RunResult &rr);
+int sm_count_of(ptg_ctx *ctx);
+
+}  // namespace ptg

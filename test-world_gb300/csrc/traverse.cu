@@ -1,0 +1,626 @@
+// traverse.cu - frontier traversal engine: BFS (direction-optimizing), SSSP
+// (near/far buckets over integer atomicMin), CC min-label propagation, and the
+// out-of-core partition streamer they share.
+//
+// Reference path replaced (ptGraph/main.cu):
+//   bfsCaculateInOpt 1180-1418, bfsCaculateInAsync 1420-1678,
+//   bfsCaculateInAsyncSwap 1681-2059, bfsCaculateInShare 1041-1123,
+//   ssspCaculateInOpt 678-889, ssspCaculateInShare 563-638,
+//   ccCaculateInOpt 222-440, ccCaculateInShare 961-1035.
+// Kernels replaced (ptGraph/gpu_kernels.cu): the relax kernels 118-448 (one
+// atomicMin + label per improved target), the compaction kernels 3-116 plus
+// Thrust reduce/exclusive_scan over all n vertices every round, and the
+// fragment kernels 450-485.
+//
+// What changes on GB300:
+//  * The frontier is a compact queue plus a bitmap, built by the relax kernel
+//    itself (warp-aggregated appends, bitmap dedup), so no O(n) label scan is
+//    needed per round (reference: setLabeling + scan + compaction over n).
+//  * Edges are expanded load-balanced: the frontier's degrees are scanned,
+//    and each 256-thread CTA takes a 2048-edge tile of the flattened edge
+//    space; consecutive threads read consecutive edges of one adjacency list
+//    (coalesced), a hub's edges spread over many CTAs (reference: one thread
+//    walks a whole adjacency list, gpu_kernels.cu:126).
+//  * BFS switches to bottom-up rounds (each unvisited vertex looks for a
+//    parent in the frontier bitmap) when the frontier's edges outweigh the
+//    unvisited edges (Beamer's direction optimization).
+//  * SSSP keeps a near frontier below a moving threshold and a far pile above
+//    it, so vertices are expanded close to their final distance instead of
+//    every time they improve (reference: Bellman-Ford rounds, main.cu:799-863).
+//  * Out-of-core: edges past the resident prefix live in pinned host memory
+//    and are cut into fixed-size partitions.  Each round only partitions that
+//    hold an active vertex's edges are copied (cudaMemcpyAsync on a copy
+//    stream into 2-3 staging buffers, ordered with events) and relaxed
+//    edge-centrically; the rest are skipped (reference: 20 CPU threads gather
+//    active adjacency into a unified-memory buffer the GPU page-faults on,
+//    main.cu:1126-1156, 1336-1378).
+#include <algorithm>
+#include <cstring>
+
+#include "ptg_device.cuh"
+
+namespace ptg {
+namespace {
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+__global__ void k_fill_u32(uint32_t *a, uint64_t n, uint32_t v) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        a[i] = v;
+}
+
+__global__ void k_iota_u32(uint32_t *a, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        a[i] = (uint32_t)i;
+}
+
+__global__ void k_fill_bits(uint32_t *bm, uint64_t n) {
+    uint64_t words = (n + 31) / 32;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < words;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t left = n - i * 32;
+        bm[i] = left >= 32 ? 0xffffffffu : ((1u << left) - 1u);
+    }
+}
+
+// Seed a single-source frontier.
+__global__ void k_seed(uint32_t *value, uint32_t src, uint32_t base, uint32_t *q, uint32_t *bm,
+                       TravCtl *ctl) {
+    value[src] = base;
+    q[0] = src;
+    bm[src >> 5] |= 1u << (src & 31u);
+    ctl->F = 1;
+}
+
+// Degree of frontier entry i, clipped to the resident edge prefix.
+template <class OffT>
+__device__ __forceinline__ OffT clipped_degree(const OffT *off, uint32_t u, OffT clip, OffT &start) {
+    OffT b = off[u], e = off[u + 1];
+    start = b;
+    if (e > clip) e = clip;
+    return e > b ? (OffT)(e - b) : (OffT)0;
+}
+
+// Pass 1 of the frontier degree scan: per-CTA sums over contiguous slices.
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_scan_reduce(const uint32_t *q, const TravCtl *ctl,
+                                                        const OffT *off, OffT clip,
+                                                        unsigned long long *bsum) {
+    uint64_t F = ctl->F;
+    uint64_t per = (F + gridDim.x - 1) / gridDim.x;
+    uint64_t lo = min(F, (uint64_t)blockIdx.x * per), hi = min(F, lo + per);
+    unsigned long long s = 0;
+    for (uint64_t i = lo + threadIdx.x; i < hi; i += kBlock) {
+        OffT st;
+        s += clipped_degree(off, q[i], clip, st);
+    }
+    s = block_reduce_sum(s);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = s;
+}
+
+// Pass 2: one CTA turns the per-CTA sums into exclusive offsets; ctl->E = total.
+__global__ void __launch_bounds__(kBlock) k_scan_bsums(unsigned long long *bsum, int nb,
+                                                       TravCtl *ctl) {
+    unsigned long long carry = 0;
+    for (int base = 0; base < nb; base += kBlock) {
+        int i = base + threadIdx.x;
+        unsigned long long x = i < nb ? bsum[i] : 0ull, tot;
+        unsigned long long ex = block_exclusive_scan(x, tot);
+        if (i < nb) bsum[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) {
+        ctl->E = carry;
+        ctl->edges_done += carry;
+    }
+}
+
+// Pass 3: per-CTA scan of its slice; writes sc[i] (exclusive prefix of the
+// clipped degrees), rs[i] (adjacency start of q[i]) and sc[F] = E.
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_scan_write(const uint32_t *q, const TravCtl *ctl,
+                                                       const OffT *off, OffT clip,
+                                                       const unsigned long long *bsum, OffT *sc,
+                                                       OffT *rs) {
+    uint64_t F = ctl->F;
+    uint64_t per = (F + gridDim.x - 1) / gridDim.x;
+    uint64_t lo = min(F, (uint64_t)blockIdx.x * per), hi = min(F, lo + per);
+    unsigned long long run = bsum[blockIdx.x];
+    for (uint64_t base = lo; base < hi; base += kBlock) {
+        uint64_t i = base + threadIdx.x;
+        OffT d = 0, st = 0;
+        if (i < hi) d = clipped_degree(off, q[i], clip, st);
+        unsigned long long tot;
+        unsigned long long ex = block_exclusive_scan((unsigned long long)d, tot);
+        if (i < hi) {
+            sc[i] = (OffT)(run + ex);
+            rs[i] = st;
+        }
+        run += tot;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc[F] = (OffT)ctl->E;
+}
+
+struct PushTargets {
+    uint32_t *value;
+    uint32_t *q_next;
+    uint32_t *bm_next;
+    uint32_t *far_q;   // nullptr: no far pile
+    uint32_t *far_bm;
+    TravCtl *ctl;
+    uint32_t cap;      // queue capacity (n)
+};
+
+// Relax one edge: the reference's rule (gpu_kernels.cu:126-131), plus the
+// near/far routing and bitmap dedup of the next frontier.
+__device__ __forceinline__ void relax(const PushTargets &t, uint32_t v, uint32_t nd,
+                                      uint32_t threshold) {
+    if (nd < t.value[v]) {
+        uint32_t old = atomicMin(&t.value[v], nd);
+        if (nd < old) {
+            uint32_t bit = 1u << (v & 31u);
+            if (nd < threshold || t.far_q == nullptr) {
+                uint32_t prev = atomicOr(&t.bm_next[v >> 5], bit);
+                if (!(prev & bit)) {
+                    warp_append(t.q_next, &t.ctl->next_tail, t.cap, &t.ctl->error, v);
+                    if (t.far_bm && (t.far_bm[v >> 5] & bit)) atomicAnd(&t.far_bm[v >> 5], ~bit);
+                }
+            } else {
+                uint32_t prev = atomicOr(&t.far_bm[v >> 5], bit);
+                if (!(prev & bit))
+                    warp_append(t.far_q, &t.ctl->far_count, t.cap, &t.ctl->error, v);
+            }
+        }
+    }
+}
+
+// Load-balanced top-down expansion of the frontier's (resident) edges.
+// mode: 0 BFS (+1), 1 SSSP (+w), 2 CC (propagate value).
+template <class OffT, int MODE>
+__global__ void __launch_bounds__(kBlock) k_expand(const uint32_t *q, const OffT *sc, const OffT *rs,
+                                                   const uint32_t *col, const uint32_t *w,
+                                                   PushTargets t) {
+    __shared__ OffT s_sc[kTile + 1];
+    __shared__ OffT s_rs[kTile + 1];
+    __shared__ uint32_t s_val[kTile + 1];
+    __shared__ uint64_t s_r0, s_nrows;
+    const TravCtl *ctl = t.ctl;
+    uint64_t F = ctl->F;
+    uint64_t E = ctl->E;
+    uint32_t thr = ctl->threshold;
+    uint64_t ntiles = (E + kTile - 1) / kTile;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        uint64_t t0 = tile * kTile, t1 = min(E, t0 + kTile);
+        if (threadIdx.x == 0) {
+            uint64_t r0 = last_le(sc, 0, F, t0);
+            uint64_t r1 = last_le(sc, r0, F, t1 - 1);
+            s_r0 = r0;
+            s_nrows = r1 - r0 + 1;
+        }
+        __syncthreads();
+        uint64_t r0 = s_r0, nrows = s_nrows;
+        bool staged = nrows <= (uint64_t)kTile;
+        if (staged) {
+            for (uint64_t k = threadIdx.x; k < nrows; k += kBlock) {
+                s_sc[k] = sc[r0 + k];
+                s_rs[k] = rs[r0 + k];
+                s_val[k] = t.value[q[r0 + k]];
+            }
+            if (threadIdx.x == 0) s_sc[nrows] = sc[r0 + nrows];
+        }
+        __syncthreads();
+        for (uint64_t j = t0 + threadIdx.x; j < t1; j += kBlock) {
+            uint64_t row;
+            OffT rsv, scv;
+            uint32_t uval;
+            if (staged) {
+                row = last_le(s_sc, 0, nrows, j);
+                rsv = s_rs[row];
+                scv = s_sc[row];
+                uval = s_val[row];
+            } else {
+                row = last_le(sc, r0, r0 + nrows, j);
+                rsv = rs[row];
+                scv = sc[row];
+                uval = t.value[q[row]];
+            }
+            uint64_t e = (uint64_t)rsv + (j - (uint64_t)scv);
+            uint32_t v = col[e];
+            uint32_t nd = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + w[e] : uval);
+            relax(t, v, nd, thr);
+        }
+        __syncthreads();
+    }
+}
+
+// Bottom-up BFS round (symmetric graphs): each unvisited vertex scans its
+// neighbours for one in the current frontier bitmap.  A warp owns 32
+// consecutive vertices, so it writes its word of the next bitmap with one
+// store (ballot) and appends its discoveries with one atomic.
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_bottom_up(uint64_t n, const OffT *off,
+                                                      const uint32_t *col, const uint32_t *bm_cur,
+                                                      PushTargets t) {
+    uint32_t newval = t.ctl->level_val + 1u;
+    uint64_t nwarps_total = (uint64_t)gridDim.x * (kBlock / 32);
+    uint64_t wglobal = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5);
+    uint64_t words = (n + 31) / 32;
+    for (uint64_t wd = wglobal; wd < words; wd += nwarps_total) {
+        uint64_t v = wd * 32 + lane_id();
+        bool found = false;
+        if (v < n && t.value[v] == PTG_UNREACHED) {
+            OffT b = off[v], e = off[v + 1];
+            for (OffT k = b; k < e; k++) {
+                if (bit_test(bm_cur, col[k])) {
+                    found = true;
+                    break;
+                }
+            }
+        }
+        unsigned ballot = __ballot_sync(0xffffffffu, found);
+        if (lane_id() == 0 && ballot) t.bm_next[wd] = ballot;
+        if (found) {
+            t.value[v] = newval;
+            warp_append(t.q_next, &t.ctl->next_tail, t.cap, &t.ctl->error, (uint32_t)v);
+        }
+    }
+}
+
+// Out-of-core: mark the streamed partitions that hold edges of frontier
+// vertices (the reference's setFragmentData, gpu_kernels.cu:450-462, which
+// flags 4096-edge fragments of active vertices).
+template <class OffT>
+__global__ void k_mark_partitions(const uint32_t *q, const TravCtl *ctl, const OffT *off,
+                                  uint64_t resident_edges, uint64_t part_edges,
+                                  uint64_t resident_parts, uint64_t nparts, uint8_t *flags) {
+    uint64_t F = ctl->F;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < F;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t u = q[i];
+        uint64_t b = off[u], e = off[u + 1];
+        if (e <= resident_edges || e <= b) continue;
+        if (b < resident_edges) b = resident_edges;
+        uint64_t p0 = b / part_edges, p1 = (e - 1) / part_edges;
+        for (uint64_t p = p0; p <= p1 && p < nparts; p++)
+            if (p >= resident_parts && !flags[p]) flags[p] = 1;
+    }
+}
+
+// Out-of-core: relax every edge of one staged partition whose source vertex
+// is in the frontier bitmap.  Edge-centric tiles; the source row of each edge
+// is found by binary search over the tile's offsets (staged in shared memory).
+template <class OffT, int MODE>
+__global__ void __launch_bounds__(kBlock) k_relax_partition(uint64_t e_begin, uint64_t e_end,
+                                                            uint64_t v_first, uint64_t v_last,
+                                                            const OffT *off,
+                                                            const uint32_t *stage_col,
+                                                            const uint32_t *stage_w,
+                                                            const uint32_t *bm_cur, PushTargets t) {
+    __shared__ OffT s_off[kTile + 2];
+    __shared__ uint32_t s_val[kTile + 1];
+    __shared__ uint64_t s_r0, s_nrows;
+    uint32_t thr = t.ctl->threshold;
+    uint64_t E = e_end - e_begin;
+    uint64_t ntiles = (E + kTile - 1) / kTile;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        uint64_t t0 = e_begin + tile * kTile, t1 = min(e_end, t0 + kTile);
+        if (threadIdx.x == 0) {
+            uint64_t r0 = last_le(off, v_first, v_last + 1, t0);
+            uint64_t r1 = last_le(off, r0, v_last + 1, t1 - 1);
+            s_r0 = r0;
+            s_nrows = r1 - r0 + 1;
+        }
+        __syncthreads();
+        uint64_t r0 = s_r0, nrows = s_nrows;
+        bool staged = nrows <= (uint64_t)kTile;
+        if (staged) {
+            for (uint64_t k = threadIdx.x; k < nrows; k += kBlock) {
+                uint32_t u = (uint32_t)(r0 + k);
+                s_off[k] = off[u];
+                s_val[k] = bit_test(bm_cur, u) ? t.value[u] : PTG_UNREACHED;
+            }
+            if (threadIdx.x == 0) s_off[nrows] = off[r0 + nrows];
+        }
+        __syncthreads();
+        for (uint64_t j = t0 + threadIdx.x; j < t1; j += kBlock) {
+            uint32_t uval;
+            if (staged) {
+                uint64_t row = last_le(s_off, 0, nrows, j);
+                uval = s_val[row];
+            } else {
+                uint64_t u = last_le(off, r0, r0 + nrows, j);
+                uval = bit_test(bm_cur, (uint32_t)u) ? t.value[u] : PTG_UNREACHED;
+            }
+            if (uval == PTG_UNREACHED) continue;
+            uint64_t le = j - e_begin;
+            uint32_t v = stage_col[le];
+            uint32_t nd = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + stage_w[le] : uval);
+            relax(t, v, nd, thr);
+        }
+        __syncthreads();
+    }
+}
+
+// Near/far: smallest live distance in the far pile.
+__global__ void __launch_bounds__(kBlock) k_far_min(const uint32_t *far_q, const uint32_t *far_bm,
+                                                    const uint32_t *value, TravCtl *ctl) {
+    uint32_t cnt = ctl->far_count;
+    uint32_t best = PTG_UNREACHED;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t v = far_q[i];
+        if (bit_test(far_bm, v)) best = min(best, value[v]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_down_sync(0xffffffffu, best, o));
+    if (lane_id() == 0 && best != PTG_UNREACHED) atomicMin(&ctl->far_min, (unsigned long long)best);
+}
+
+// Near/far: move far entries below the new threshold into the (empty) near
+// frontier, keep the rest, drop entries that already moved to near.
+__global__ void __launch_bounds__(kBlock) k_far_split(const uint32_t *far_in, uint32_t *far_out,
+                                                      uint32_t *far_bm, const uint32_t *value,
+                                                      uint32_t *q, uint32_t *bm, TravCtl *ctl,
+                                                      uint32_t cap) {
+    uint32_t cnt = ctl->far_count;
+    uint32_t thr = ctl->threshold;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t v = far_in[i];
+        uint32_t bit = 1u << (v & 31u);
+        if (!(far_bm[v >> 5] & bit)) continue;
+        if (value[v] < thr) {
+            atomicAnd(&far_bm[v >> 5], ~bit);
+            uint32_t prev = atomicOr(&bm[v >> 5], bit);
+            if (!(prev & bit)) warp_append(q, &ctl->next_tail, cap, &ctl->error, v);
+        } else {
+            warp_append(far_out, &ctl->far_tail, cap, &ctl->error, v);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+template <class OffT>
+void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value, uint32_t flags,
+                   uint32_t delta, uint32_t max_iters, RunResult &rr) {
+    ptg_ctx *ctx = g->ctx;
+    Workspace &ws = ctx->ws;
+    cudaStream_t st = ctx->stream;
+    const uint64_t n = g->n;
+    const int sms = ctx->sm_count;
+    const uint64_t words = (n + 31) / 32;
+
+    ws.q[0].ensure(n * 4);
+    ws.q[1].ensure(n * 4);
+    ws.bm[0].ensure(words * 4);
+    ws.bm[1].ensure(words * 4);
+    ws.scan.ensure((n + 1) * sizeof(OffT));
+    ws.rowstart.ensure((n + 1) * sizeof(OffT));
+    const int kScanBlocks = 1024;
+    ws.bsum.ensure(kScanBlocks * 8);
+    ws.ctl.ensure(sizeof(TravCtl));
+    ws.h_ctl.ensure(sizeof(TravCtl));
+    bool use_far = kind == TRAV_SSSP && !(flags & PTG_REFERENCE_SCHEDULE);
+    if (use_far) {
+        ws.farq[0].ensure(n * 4);
+        ws.farq[1].ensure(n * 4);
+        ws.farbm.ensure(words * 4);
+    }
+    TravCtl *d_ctl = ws.ctl.as<TravCtl>();
+    TravCtl *h_ctl = ws.h_ctl.as<TravCtl>();
+    const OffT *off = g->d_off.as<OffT>();
+    const uint32_t *col = g->d_col.as<uint32_t>();
+    const uint32_t *wt = g->d_w.as<uint32_t>();
+    OffT clip = (OffT)g->resident_edges;
+
+    // ---- initial state ----
+    TravCtl init{};
+    init.threshold = PTG_UNREACHED;
+    init.m_unvisited = g->m;
+    PTG_CUDA_TRY(cudaMemsetAsync(ws.bm[0].p, 0, words * 4, st));
+    PTG_CUDA_TRY(cudaMemsetAsync(ws.bm[1].p, 0, words * 4, st));
+    uint32_t base = (flags & PTG_LEVEL_ZERO_BASED) ? 0u : 1u;
+    int fill_grid = grid_for(n, kBlock, sms * 8);
+    if (kind == TRAV_CCPROP) {
+        launch(ctx, "k_iota_u32", k_iota_u32, fill_grid, kBlock, 0, st, d_value, n);
+        launch(ctx, "k_iota_u32", k_iota_u32, fill_grid, kBlock, 0, st, ws.q[0].as<uint32_t>(), n);
+        launch(ctx, "k_fill_bits", k_fill_bits, grid_for(words, kBlock, sms * 8), kBlock, 0, st,
+               ws.bm[0].as<uint32_t>(), n);
+        init.F = (uint32_t)n;
+    } else {
+        launch(ctx, "k_fill_u32", k_fill_u32, fill_grid, kBlock, 0, st, d_value, n, PTG_UNREACHED);
+        init.F = 1;
+        init.level_val = base;
+        if (use_far) {
+            if (delta == 0) delta = 64;
+            init.threshold = base + delta;
+            PTG_CUDA_TRY(cudaMemsetAsync(ws.farbm.p, 0, words * 4, st));
+        }
+    }
+    PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &init, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
+    if (kind != TRAV_CCPROP)
+        launch(ctx, "k_seed", k_seed, 1, 1, 0, st, d_value, src, base, ws.q[0].as<uint32_t>(),
+               ws.bm[0].as<uint32_t>(), d_ctl);
+    PTG_CUDA_TRY(cudaGetLastError());
+
+    bool allow_bu = kind == TRAV_BFS && g->symmetric && !g->out_of_core &&
+                    !(flags & (PTG_NO_DIRECTION_OPT | PTG_REFERENCE_SCHEDULE));
+    int cur = 0, far_cur = 0;
+    uint64_t F = init.F, far_count = 0, m_unvisited = g->m;
+    uint32_t threshold = init.threshold, level_val = base;
+    bool bottom_up = false;
+    if (max_iters == 0) max_iters = (uint32_t)std::min<uint64_t>(0xFFFFFFF0ull, 4 * n + 16);
+    const double alpha = 15.0, beta = 18.0;
+
+    // out-of-core staging
+    if (g->out_of_core) {
+        ws.flags.ensure(g->num_partitions);
+        ws.h_flags.ensure(g->num_partitions);
+    }
+    uint8_t *h_flags = ws.h_flags.as<uint8_t>();
+    int stage_next = 0;
+
+    while (true) {
+        if (F == 0) {
+            if (!use_far || far_count == 0) break;
+            // advance the threshold past the smallest far distance
+            unsigned long long big = ~0ull;
+            PTG_CUDA_TRY(cudaMemcpyAsync(&d_ctl->far_min, &big, 8, cudaMemcpyHostToDevice, st));
+            launch(ctx, "k_far_min", k_far_min, grid_for(far_count, kBlock, sms * 4), kBlock, 0, st,
+                   ws.farq[far_cur].as<uint32_t>(), ws.farbm.as<uint32_t>(), d_value, d_ctl);
+            PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
+            PTG_CUDA_TRY(cudaStreamSynchronize(st));
+            if (h_ctl->far_min == ~0ull) break;  // only stale entries left
+            uint64_t thr64 = h_ctl->far_min + delta;
+            threshold = thr64 >= PTG_UNREACHED ? PTG_UNREACHED : (uint32_t)thr64;
+            TravCtl upd = *h_ctl;
+            upd.threshold = threshold;
+            upd.next_tail = 0;
+            upd.far_tail = 0;
+            PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &upd, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
+            // bm[cur] is clear (it was the previous round's empty next bitmap)
+            launch(ctx, "k_far_split", k_far_split, grid_for(far_count, kBlock, sms * 8), kBlock, 0, st,
+                ws.farq[far_cur].as<uint32_t>(), ws.farq[far_cur ^ 1].as<uint32_t>(),
+                ws.farbm.as<uint32_t>(), d_value, ws.q[cur].as<uint32_t>(), ws.bm[cur].as<uint32_t>(),
+                d_ctl, (uint32_t)n);
+            PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
+            PTG_CUDA_TRY(cudaStreamSynchronize(st));
+            PTG_REQUIRE(h_ctl->error == 0, PTG_ERR_CUDA, "frontier overflow in far split");
+            F = h_ctl->next_tail;
+            far_count = h_ctl->far_tail;
+            far_cur ^= 1;
+            upd = *h_ctl;
+            upd.F = (uint32_t)F;
+            upd.far_count = (uint32_t)far_count;
+            upd.next_tail = 0;
+            upd.far_tail = 0;
+            PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &upd, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
+            continue;
+        }
+        if (rr.iterations >= max_iters) throw Error{PTG_ERR_TIMEOUT, "iteration limit reached"};
+        rr.iterations++;
+        uint32_t *q_cur = ws.q[cur].as<uint32_t>(), *q_nxt = ws.q[cur ^ 1].as<uint32_t>();
+        uint32_t *bm_cur = ws.bm[cur].as<uint32_t>(), *bm_nxt = ws.bm[cur ^ 1].as<uint32_t>();
+        PTG_CUDA_TRY(cudaMemsetAsync(bm_nxt, 0, words * 4, st));
+        PushTargets pt{d_value, q_nxt, bm_nxt, use_far ? ws.farq[far_cur].as<uint32_t>() : nullptr,
+                       use_far ? ws.farbm.as<uint32_t>() : nullptr, d_ctl, (uint32_t)n};
+        int scan_blocks = grid_for(F, kBlock, kScanBlocks);
+        unsigned long long *bsum = ws.bsum.as<unsigned long long>();
+        OffT *sc = ws.scan.as<OffT>(), *rs = ws.rowstart.as<OffT>();
+
+        // direction decision needs the frontier's edge count first
+        launch(ctx, "k_scan_reduce", k_scan_reduce<OffT>, scan_blocks, kBlock, 0, st, q_cur, d_ctl, off,
+               clip, bsum);
+        launch(ctx, "k_scan_bsums", k_scan_bsums, 1, kBlock, 0, st, bsum, scan_blocks, d_ctl);
+        uint64_t E = 0;
+        if (allow_bu) {
+            PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
+            PTG_CUDA_TRY(cudaStreamSynchronize(st));
+            E = h_ctl->E;
+            if (!bottom_up && (double)E > (double)m_unvisited / alpha) bottom_up = true;
+            else if (bottom_up && (double)F < (double)n / beta) bottom_up = false;
+            m_unvisited = m_unvisited > E ? m_unvisited - E : 0;
+        }
+        if (bottom_up) {
+            rr.bottom_up_rounds++;
+            if (h_ctl->level_val != level_val) {
+                PTG_CUDA_TRY(cudaMemcpyAsync(&d_ctl->level_val, &level_val, 4, cudaMemcpyHostToDevice, st));
+            }
+            launch(ctx, "k_bottom_up", k_bottom_up<OffT>, grid_for(words * 32, kBlock, sms * 16), kBlock, 0,
+                   st, n, off, col, bm_cur, pt);
+        } else {
+            launch(ctx, "k_scan_write", k_scan_write<OffT>, scan_blocks, kBlock, 0, st, q_cur, d_ctl, off,
+                   clip, bsum, sc, rs);
+            int eg = sms * 8;
+            if (allow_bu) eg = grid_for(E, kTile, sms * 8);
+            if (kind == TRAV_BFS)
+                launch(ctx, "k_expand_bfs", k_expand<OffT, 0>, eg, kBlock, 0, st, q_cur, sc, rs, col, wt, pt);
+            else if (kind == TRAV_SSSP)
+                launch(ctx, "k_expand_sssp", k_expand<OffT, 1>, eg, kBlock, 0, st, q_cur, sc, rs, col, wt, pt);
+            else
+                launch(ctx, "k_expand_cc", k_expand<OffT, 2>, eg, kBlock, 0, st, q_cur, sc, rs, col, wt, pt);
+            PTG_CUDA_TRY(cudaGetLastError());
+            if (g->out_of_core) {
+                // stream the active partitions past the resident prefix
+                uint8_t *d_flags = ws.flags.as<uint8_t>();
+                PTG_CUDA_TRY(cudaMemsetAsync(d_flags, 0, g->num_partitions, st));
+                launch(ctx, "k_mark_partitions", k_mark_partitions<OffT>, grid_for(F, kBlock, sms * 8), kBlock,
+                       0, st, q_cur, d_ctl, off, g->resident_edges, g->partition_edges,
+                       g->resident_partitions, g->num_partitions, d_flags);
+                PTG_CUDA_TRY(cudaMemcpyAsync(h_flags, d_flags, g->num_partitions, cudaMemcpyDeviceToHost, st));
+                PTG_CUDA_TRY(cudaStreamSynchronize(st));
+                for (uint64_t p = g->resident_partitions; p < g->num_partitions; p++) {
+                    if (!h_flags[p]) {
+                        rr.parts_skipped++;
+                        continue;
+                    }
+                    uint64_t e0 = p * g->partition_edges;
+                    uint64_t e1 = std::min<uint64_t>(g->m, e0 + g->partition_edges);
+                    int b = stage_next;
+                    stage_next = (stage_next + 1) % (int)g->n_stage;
+                    cudaStream_t cs = ctx->copy_stream;
+                    PTG_CUDA_TRY(cudaStreamWaitEvent(cs, g->stage_free[b], 0));
+                    PTG_CUDA_TRY(cudaMemcpyAsync(g->stage_col[b].p, g->h_col + e0, (e1 - e0) * 4,
+                                                 cudaMemcpyHostToDevice, cs));
+                    rr.link_bytes += (e1 - e0) * 4;
+                    if (kind == TRAV_SSSP) {
+                        PTG_CUDA_TRY(cudaMemcpyAsync(g->stage_w[b].p, g->h_w + e0, (e1 - e0) * 4,
+                                                     cudaMemcpyHostToDevice, cs));
+                        rr.link_bytes += (e1 - e0) * 4;
+                    }
+                    PTG_CUDA_TRY(cudaEventRecord(g->stage_ready[b], cs));
+                    PTG_CUDA_TRY(cudaStreamWaitEvent(st, g->stage_ready[b], 0));
+                    uint64_t vf = g->part_first_vertex[p], vl = g->part_first_vertex[p + 1];
+                    int pg = grid_for(e1 - e0, kTile, sms * 8);
+                    const uint32_t *sc_ = g->stage_col[b].as<uint32_t>();
+                    const uint32_t *sw_ = g->stage_w[b].as<uint32_t>();
+                    if (kind == TRAV_BFS)
+                        launch(ctx, "k_relax_partition_bfs", k_relax_partition<OffT, 0>, pg, kBlock, 0, st, e0,
+                               e1, vf, vl, off, sc_, sw_, bm_cur, pt);
+                    else if (kind == TRAV_SSSP)
+                        launch(ctx, "k_relax_partition_sssp", k_relax_partition<OffT, 1>, pg, kBlock, 0, st, e0,
+                               e1, vf, vl, off, sc_, sw_, bm_cur, pt);
+                    else
+                        launch(ctx, "k_relax_partition_cc", k_relax_partition<OffT, 2>, pg, kBlock, 0, st, e0,
+                               e1, vf, vl, off, sc_, sw_, bm_cur, pt);
+                    PTG_CUDA_TRY(cudaGetLastError());
+                    PTG_CUDA_TRY(cudaEventRecord(g->stage_free[b], st));
+                    rr.parts_streamed++;
+                    if (g->resident_policy == PTG_RESIDENT_HOT && p < g->part_visits.size())
+                        g->part_visits[p]++;
+                }
+            }
+        }
+        // next frontier
+        PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
+        PTG_CUDA_TRY(cudaStreamSynchronize(st));
+        PTG_REQUIRE(h_ctl->error == 0, PTG_ERR_CUDA, "frontier overflow in relax");
+        F = h_ctl->next_tail;
+        if (use_far) far_count = h_ctl->far_count;
+        TravCtl upd = *h_ctl;
+        upd.F = (uint32_t)F;
+        upd.next_tail = 0;
+        level_val++;
+        upd.level_val = level_val;
+        PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &upd, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
+        cur ^= 1;
+    }
+    PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
+    PTG_CUDA_TRY(cudaStreamSynchronize(st));
+    rr.edges_relaxed = h_ctl->edges_done;
+}
+
+}  // namespace
+
+void run_traversal(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value, uint32_t flags,
+                   uint32_t delta, uint32_t max_iters, RunResult &rr) {
+    if (g->off64) traverse_impl<unsigned long long>(g, kind, src, d_value, flags, delta, max_iters, rr);
+    else traverse_impl<uint32_t>(g, kind, src, d_value, flags, delta, max_iters, rr);
+}
+
+}  // namespace ptg

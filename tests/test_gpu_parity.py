@@ -1,0 +1,221 @@
+"""GPU parity: the CUDA engine (through the C ABI) against the reference's own
+results (golden fixtures) and the CPU oracle.  Integer results are bit-exact;
+PageRank is within 1e-6 max relative error of the FP64 oracle."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLD = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+IDS = [os.path.basename(p)[:-4] for p in GOLD]
+UMAX = 0xFFFFFFFF
+PR_RTOL = 1e-6  # max per-vertex relative error vs the FP64 oracle
+
+
+def load(path):
+    z = np.load(path)
+    return {k: z[k] for k in z.files}
+
+
+# partition configurations: resident, and out-of-core with tiny partitions
+# (about 12 partitions per graph, 8 bytes per weighted edge)
+def configs(ptg, m):
+    pb = max(32, (m * 8 // 12) // 8 * 8)
+    return {
+        "resident": None,
+        "ooc_prefix": ptg.partition_config(partition_bytes=pb, device_budget_bytes=4 * pb,
+                                           force_out_of_core=1),
+        "ooc_none_3buf": ptg.partition_config(partition_bytes=pb, device_budget_bytes=1 << 20,
+                                              force_out_of_core=1, n_staging_buffers=3,
+                                              resident_policy=ptg.PTG_RESIDENT_NONE),
+    }
+
+
+@pytest.mark.parametrize("path", GOLD, ids=IDS)
+@pytest.mark.parametrize("cfgname", ["resident", "ooc_prefix", "ooc_none_3buf"])
+def test_bfs_sssp_cc_match_reference(ptg, ctx, path, cfgname):
+    g = load(path)
+    sym = bool(g["symmetric"][0])
+    cfg = configs(ptg, g["col"].size)[cfgname]
+    G = ctx.graph(g["off"], g["col"], g["w"], symmetric=sym, config=cfg)
+    info = G.info()
+    if cfgname != "resident" and g["col"].size > 16:
+        assert info["out_of_core"] == 1
+    for i, s in enumerate(g["sources"]):
+        s = int(s)
+        assert (G.bfs(s) == g["bfs"][i]).all()
+        assert (G.bfs(s, flags=ptg.PTG_NO_DIRECTION_OPT) == g["bfs"][i]).all()
+        assert (G.bfs(s, flags=ptg.PTG_REFERENCE_SCHEDULE) == g["bfs"][i]).all()
+        if "sssp" in g:
+            assert (G.sssp(s) == g["sssp"][i]).all()
+            assert (G.sssp(s, delta=1) == g["sssp"][i]).all()
+            assert (G.sssp(s, flags=ptg.PTG_REFERENCE_SCHEDULE) == g["sssp"][i]).all()
+            assert (G.sssp(s, flags=ptg.PTG_UNREACHED_MINUS1) == g["sssp_share"][i]).all()
+    assert (G.cc() == g["cc"]).all()
+    assert (G.cc(flags=ptg.PTG_REFERENCE_SCHEDULE) == g["cc"]).all()
+    G.close()
+
+
+@pytest.mark.parametrize("path", GOLD, ids=IDS)
+def test_drop_in_entry_points_match_reference(ptg, path):
+    g = load(path)
+    off_n = g["off"][:-1].astype(np.uint32)
+    col, w = g["col"], g["w"]
+    if col.size == 0:
+        col = np.zeros(0, dtype=np.uint32)
+    s = int(g["sources"][-1])
+    for name in ["bfsCaculateInOpt", "bfsCaculateInAsync", "bfsCaculateInAsyncSwap", "bfsCaculateInShare"]:
+        ms, out = ptg.compat.run(name, off_n, col, s)
+        assert ms >= 0
+        assert (out == g["bfs"][-1]).all(), name
+    if col.size:
+        aos = np.stack([col, w], axis=1).astype(np.uint32)
+        _, out = ptg.compat.run("ssspCaculateInOpt", off_n, aos, s)
+        assert (out == g["sssp"][-1]).all()
+        _, out = ptg.compat.run("ssspCaculateInShare", off_n, aos, s)
+        assert (out == g["sssp_share"][-1]).all()
+    for name in ["ccCaculateInOpt", "ccCaculateInShare"]:
+        _, out = ptg.compat.run(name, off_n, col)
+        assert (out == g["cc"]).all(), name
+    _, out = ptg.compat.run("caculateInCommon", off_n, col)
+    assert (out == g["bfs_common_src0"]).all()
+    _, out = ptg.compat.run("caculateInShareOpt", off_n, col)
+    assert (out == g["bfs_shareopt"]).all()
+    _, out = ptg.compat.run("caculateInOptChooseByDegree", off_n, col, s)
+    assert (out == g["bfs"][-1]).all()
+
+
+def test_drop_in_out_of_core_config(ptg):
+    g = load(os.path.join(os.path.dirname(__file__), "golden", "rmat12_sym.npz"))
+    ptg.compat.set_partition_config(ptg.partition_config(partition_bytes=4096, device_budget_bytes=40000,
+                                                         force_out_of_core=1))
+    try:
+        off_n = g["off"][:-1].astype(np.uint32)
+        for i, s in enumerate(g["sources"]):
+            _, out = ptg.compat.run("bfsCaculateInOpt", off_n, g["col"], int(s))
+            assert (out == g["bfs"][i]).all()
+        aos = np.stack([g["col"], g["w"]], axis=1).astype(np.uint32)
+        _, out = ptg.compat.run("ssspCaculateInOpt", off_n, aos, int(g["sources"][0]))
+        assert (out == g["sssp"][0]).all()
+        _, out = ptg.compat.run("ccCaculateInOpt", off_n, g["col"])
+        assert (out == g["cc"]).all()
+    finally:
+        ptg.compat.set_partition_config(None)
+
+
+@pytest.mark.parametrize("name", ["rmat8_sym", "rmat10_sym", "rmat12_sym", "path10", "star20",
+                                  "two_comp_isolated", "single_vertex", "no_edges"])
+def test_pagerank_within_tolerance(ptg, ctx, oracle, name):
+    g = load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    G = ctx.graph(g["off"], g["col"], symmetric=True)
+    r = G.pagerank().astype(np.float64)
+    ref = oracle.pagerank(g["off"], g["col"])
+    rel = np.abs(r - ref) / ref
+    assert rel.max() < PR_RTOL, rel.max()
+    for s in g["sources"][:2]:
+        p = G.ppr(int(s)).astype(np.float64)
+        pref = oracle.ppr(g["off"], g["col"], int(s))
+        nz = pref > 1e-30
+        assert (p[~nz] < 1e-30).all()
+        assert (np.abs(p[nz] - pref[nz]) / pref[nz]).max() < PR_RTOL
+    _, out = ptg.compat.run("prCaculateInShare", g["off"][:-1].astype(np.uint32), g["col"])
+    assert (np.abs(out.astype(np.float64) - ref) / ref).max() < PR_RTOL
+
+
+def test_config1_rmat16_bfs_from_vertex0(ptg, ctx, oracle):
+    """Plain BFS from vertex 0, undirected RMAT scale 16, ef 16, seed 1 (u32 CSR, u32 levels)."""
+    off, col, _ = ptg.gen_rmat(16, 16, seed=1, symmetric=True)
+    G = ctx.graph(off.astype(np.uint32), col, symmetric=True)
+    st = {}
+    lv = G.bfs(0, stats=st)
+    assert (lv == oracle.bfs(off, col, 0, method="queue")).all()
+    assert (lv == oracle.bfs(off, col, 0, method="frontier")).all()
+    off_n = off[:-1].astype(np.uint32)
+    _, out = ptg.compat.run("bfsCaculateInOpt", off_n, col, 0)
+    assert (out == lv).all()
+
+
+@pytest.mark.parametrize("scale", [14, 18])
+def test_rmat_weighted_suite_vs_oracle(ptg, ctx, oracle, scale):
+    off, col, w = ptg.gen_rmat(scale, 16, seed=2, symmetric=True, wmin=1, wmax=63)
+    G = ctx.graph(off, col, w, symmetric=True)
+    deg = np.diff(off.astype(np.int64))
+    rng = np.random.default_rng(scale)
+    srcs = rng.choice(np.nonzero(deg)[0], 4, replace=False)
+    for s in srcs:
+        s = int(s)
+        assert (G.bfs(s) == oracle.bfs(off, col, s, method="queue")).all()
+        assert (G.sssp(s) == oracle.sssp(off, col, w, s)).all()
+    assert (G.cc() == oracle.cc(off, col, method="unionfind")).all()
+    r = G.pagerank().astype(np.float64)
+    ref = oracle.pagerank(off, col)
+    assert (np.abs(r - ref) / ref).max() < PR_RTOL
+
+
+def test_directed_rmat_out_of_core_vs_oracle(ptg, ctx, oracle):
+    off, col, w = ptg.gen_rmat(14, 16, seed=3, symmetric=False, wmin=1, wmax=63)
+    cfg = ptg.partition_config(partition_bytes=1 << 16, device_budget_bytes=1 << 18, force_out_of_core=1)
+    G = ctx.graph(off, col, w, symmetric=False, config=cfg)
+    assert G.info()["out_of_core"] == 1
+    st = {}
+    d = G.sssp(0, stats=st)
+    assert (d == oracle.sssp(off, col, w, 0)).all()
+    assert st["partitions_streamed"] > 0 and st["link_bytes"] > 0
+    assert (G.bfs(0) == oracle.bfs(off, col, 0, method="queue")).all()
+    assert (G.cc() == oracle.cc(off, col)).all()
+
+
+def test_bad_arguments(ptg, ctx):
+    g = load(os.path.join(os.path.dirname(__file__), "golden", "path10.npz"))
+    G = ctx.graph(g["off"], g["col"], symmetric=True)
+    with pytest.raises(ptg.PtgError) as e:
+        G.bfs(10)
+    assert e.value.status == ptg.PTG_ERR_INVALID
+    with pytest.raises(ptg.PtgError):
+        G.sssp(0)  # unweighted graph
+    bad = g["col"].copy()
+    bad[3] = 99
+    with pytest.raises(ptg.PtgError) as e:
+        ctx.graph(g["off"], bad)
+    assert e.value.status == ptg.PTG_ERR_INVALID
+    off = g["off"].copy()
+    off[4], off[5] = off[5], off[4] + 100
+    with pytest.raises(ptg.PtgError):
+        ctx.graph(off, g["col"])
+    # still usable after errors
+    assert (G.bfs(0) == g["bfs"][0]).all()
+
+
+def test_repeated_runs_identical(ptg, ctx):
+    off, col, w = ptg.gen_rmat(15, 16, seed=5, symmetric=True, wmin=1, wmax=63)
+    G = ctx.graph(off, col, w, symmetric=True)
+    a = [G.sssp(0) for _ in range(3)] + [G.bfs(0) for _ in range(3)] + [G.cc() for _ in range(2)]
+    assert (a[0] == a[1]).all() and (a[1] == a[2]).all()
+    assert (a[3] == a[4]).all() and (a[4] == a[5]).all()
+    assert (a[6] == a[7]).all()
+
+
+def test_msbfs_equals_single_source(ptg, ctx):
+    off, col, w = ptg.gen_rmat(13, 16, seed=4, symmetric=True, wmin=1, wmax=63)
+    G = ctx.graph(off, col, w, symmetric=True)
+    srcs = np.array([0, 5, 77, 1000, 4095, 3, 3], dtype=np.uint32)
+    ms = G.msbfs(srcs)
+    for i, s in enumerate(srcs):
+        assert (ms[i] == G.bfs(int(s))).all()
+    ss = G.mssssp(srcs)
+    for i, s in enumerate(srcs):
+        assert (ss[i] == G.sssp(int(s))).all()
+
+
+def test_cc_batch_matches_per_graph(ptg, ctx, oracle):
+    vb, off, col = ptg.gen_er_batch(64, 50, 5000, 8.0, seed=11)
+    lab = ctx.cc_batch(vb, off, col)
+    for gi in range(64):
+        a, b = int(vb[gi]), int(vb[gi + 1])
+        e0, e1 = int(off[a]), int(off[b])
+        loff = (off[a:b + 1] - off[a]).astype(np.uint64)
+        lcol = (col[e0:e1] - a).astype(np.uint32)
+        assert (lab[a:b] == oracle.cc(loff, lcol, method="unionfind")).all()
