@@ -236,6 +236,31 @@ ptg_status ptg_pagerank(ptg_graph *g, float *rank, const ptg_pr_opts *opts);
 /* Personalized PageRank: teleport (and dangling mass) to src, r0 = e_src. */
 ptg_status ptg_ppr(ptg_graph *g, uint32_t src, float *rank, const ptg_pr_opts *opts);
 
+/* BFS that allocates nothing.  This entry point has no counterpart in the
+ * reference.  It is for callers that can pass device buffers but must not
+ * call cudaMalloc themselves - typically a plugin inside a host process that
+ * owns all device memory through its own pool, where a raw cudaMalloc would
+ * bypass the pool's accounting and a cudaFree would synchronize the device
+ * under the host's other work.
+ *   d_offsets : n+1 u32 offsets (sentinel form), device memory
+ *   d_col     : m u32 targets, device memory
+ *   d_levels  : n u32 outputs, device memory; same values as ptg_bfs
+ *               (level[src] = 1, unreached 0xFFFFFFFF)
+ *   stream    : a cudaStream_t (NULL = default stream); the current device
+ *               must be the one holding the buffers
+ * Its working memory is a fixed scratch area of PTG_NOALLOC_SCRATCH_BYTES
+ * inside the library, which every GPU that loads the library keeps until the
+ * process exits; graphs above PTG_NOALLOC_MAX_VERTICES vertices are rejected
+ * with PTG_ERR_UNSUPPORTED (bad pointers or src >= n: PTG_ERR_INVALID).  The
+ * first call on a device looks up the scratch's device address (make that
+ * first call before any stream capture).  All calls share the scratch, so
+ * calls that overlap on the GPU race: serialize them.  The call returns when
+ * the BFS has finished on `stream`. */
+#define PTG_NOALLOC_MAX_VERTICES (1u << 20)
+#define PTG_NOALLOC_SCRATCH_BYTES ((16u << 20) + (64u << 10))
+ptg_status ptg_bfs_noalloc(const uint32_t *d_offsets, const uint32_t *d_col, uint32_t n,
+                           uint32_t m, uint32_t src, uint32_t *d_levels, void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* Batched queries.                                                          */
 /* ------------------------------------------------------------------------ */

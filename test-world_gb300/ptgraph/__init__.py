@@ -133,6 +133,8 @@ _SIGS = {
     "ptg_cc": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(RunOpts)]),
     "ptg_pagerank": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(PrOpts)]),
     "ptg_ppr": (ctypes.c_int, [_vp, ctypes.c_uint32, _vp, ctypes.POINTER(PrOpts)]),
+    "ptg_bfs_noalloc": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp,
+                                       _vp]),
     "ptg_msbfs": (ctypes.c_int, [_vp, _u32p, ctypes.c_uint32, _vp, ctypes.POINTER(RunOpts)]),
     "ptg_mssssp": (ctypes.c_int, [_vp, _u32p, ctypes.c_uint32, _vp, ctypes.POINTER(RunOpts)]),
     "ptg_cc_batch": (ctypes.c_int, [_vp, ctypes.c_uint32, _u64p, _u64p, _u32p, _u32p,
