@@ -67,19 +67,13 @@ __global__ void __launch_bounds__(kBlock) k_hook(uint64_t e_begin, uint64_t e_en
                                                  uint64_t v_last, const OffT *off,
                                                  const uint32_t *col_base, uint32_t *parent) {
     __shared__ OffT s_off[kTile + 2];
-    __shared__ uint64_t s_r0, s_nrows;
     uint64_t E = e_end - e_begin;
     uint64_t ntiles = (E + kTile - 1) / kTile;
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         uint64_t t0 = e_begin + tile * kTile, t1 = min(e_end, t0 + kTile);
-        if (threadIdx.x == 0) {
-            uint64_t r0 = last_le(off, v_first, v_last + 1, t0);
-            uint64_t r1 = last_le(off, r0, v_last + 1, t1 - 1);
-            s_r0 = r0;
-            s_nrows = r1 - r0 + 1;
-        }
-        __syncthreads();
-        uint64_t r0 = s_r0, nrows = s_nrows;
+        uint64_t r0 = block_last_le(off, v_first, v_last + 1, t0);
+        uint64_t r1 = block_last_le(off, r0, v_last + 1, t1 - 1);
+        uint64_t nrows = r1 - r0 + 1;
         bool staged = nrows <= (uint64_t)kTile;
         if (staged) {
             for (uint64_t k = threadIdx.x; k <= nrows; k += kBlock) s_off[k] = off[r0 + k];
@@ -88,6 +82,33 @@ __global__ void __launch_bounds__(kBlock) k_hook(uint64_t e_begin, uint64_t e_en
         for (uint64_t j = t0 + threadIdx.x; j < t1; j += kBlock) {
             uint64_t u = staged ? r0 + last_le(s_off, 0, nrows, j) : last_le(off, r0, r0 + nrows, j);
             uint32_t v = col_base[j - e_begin];
+            if (v < u) hook(parent, (uint32_t)u, v);
+        }
+        __syncthreads();
+    }
+}
+
+// Hook every edge of a resident graph, tile by tile along the graph's
+// merge-path tiling (rows [i0, i1], edges [j0, j1) per tile, precomputed), so
+// no CTA searches for its rows.
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_hook_tiles(const OffT *off, const uint32_t *col,
+                                                       const uint64_t *tiles, uint64_t n, uint64_t m,
+                                                       int tile_items, uint32_t *parent) {
+    extern __shared__ unsigned char smem_raw[];
+    OffT *s_start = reinterpret_cast<OffT *>(smem_raw);
+    uint64_t total = n + m;
+    uint64_t ntiles = (total + tile_items - 1) / tile_items;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        uint64_t d0 = tile * (uint64_t)tile_items, d1 = min(total, d0 + tile_items);
+        uint64_t i0 = tiles[tile], i1 = tiles[tile + 1];
+        uint64_t j0 = d0 - i0, j1 = d1 - i1;
+        uint64_t nrows = i1 - i0;
+        for (uint64_t k = threadIdx.x; k <= nrows; k += kBlock) s_start[k] = off[i0 + k];
+        __syncthreads();
+        for (uint64_t j = j0 + threadIdx.x; j < j1; j += kBlock) {
+            uint64_t u = i0 + last_le(s_start, 0, nrows + 1, j);
+            uint32_t v = col[j];
             if (v < u) hook(parent, (uint32_t)u, v);
         }
         __syncthreads();
@@ -123,7 +144,15 @@ void cc_hook_impl(ptg_graph *g, uint32_t *d_label, RunResult &rr) {
     const OffT *off = g->d_off.as<OffT>();
     launch(ctx, "k_iota", k_iota, grid_for(n, kBlock, sms * 8), kBlock, 0, st, d_label, n, (uint64_t)0);
     uint64_t res = g->resident_edges;
-    if (res > 0) {
+    if (!g->out_of_core && res > 0) {
+        int items = merge_tile_items();
+        const uint64_t *tiles = merge_tiles(g);
+        uint64_t ntiles = (n + g->m + items - 1) / items;
+        launch(ctx, "k_hook_tiles", k_hook_tiles<OffT>, grid_for(ntiles, 1, sms * 8), kBlock,
+               (size_t)(items + 1) * sizeof(OffT), st, off, g->d_col.as<uint32_t>(), tiles, n, g->m, items,
+               d_label);
+        PTG_CUDA_TRY(cudaGetLastError());
+    } else if (res > 0) {
         uint64_t v_last = g->out_of_core ? g->part_first_vertex[g->resident_partitions] : n - 1;
         if (v_last >= n) v_last = n - 1;
         launch(ctx, "k_hook", k_hook<OffT>, grid_for(res, kTile, sms * 16), kBlock, 0, st, (uint64_t)0, res,
@@ -170,22 +199,18 @@ __global__ void __launch_bounds__(kBlock) k_hook_persistent(const unsigned long 
                                                             uint64_t m, uint32_t *parent,
                                                             unsigned long long *tile_counter) {
     __shared__ unsigned long long s_off[kTile + 2];
-    __shared__ uint64_t s_r0, s_nrows, s_tile;
+    __shared__ uint64_t s_tile;
     uint64_t ntiles = (m + kTile - 1) / kTile;
     while (true) {
         if (threadIdx.x == 0) s_tile = atomicAdd(tile_counter, 1ull);
         __syncthreads();
         uint64_t tile = s_tile;
+        __syncthreads();
         if (tile >= ntiles) break;
         uint64_t t0 = tile * kTile, t1 = min(m, t0 + kTile);
-        if (threadIdx.x == 0) {
-            uint64_t r0 = last_le(off, 0, n, t0);
-            uint64_t r1 = last_le(off, r0, n, t1 - 1);
-            s_r0 = r0;
-            s_nrows = r1 - r0 + 1;
-        }
-        __syncthreads();
-        uint64_t r0 = s_r0, nrows = s_nrows;
+        uint64_t r0 = block_last_le(off, 0, n, t0);
+        uint64_t r1 = block_last_le(off, r0, n, t1 - 1);
+        uint64_t nrows = r1 - r0 + 1;
         bool staged = nrows <= (uint64_t)kTile;
         if (staged)
             for (uint64_t k = threadIdx.x; k <= nrows; k += kBlock) s_off[k] = off[r0 + k];

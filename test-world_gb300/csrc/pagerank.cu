@@ -6,38 +6,69 @@
 //   r0 = 1/n (PPR: r0 = e_src)
 //   r' = (1-d)/n + d * (sum_{u -> v} r[u]/deg(u) + dangling/n)
 //   (PPR: r' = d * sum + [v == src] * ((1-d) + d * dangling))
-// with dangling = sum of r over zero-degree vertices, a fixed number of
-// iterations, FP32 ranks and contributions, FP64 per-vertex sums.
+// with dangling = sum of r over zero-degree vertices and a fixed number of
+// iterations.  Ranks and contributions are stored in FP32; per-vertex sums
+// are compensated two-float sums (about 48 significant bits, beyond what the
+// 1e-6 tolerance needs), because GB300 runs FP32 adds at 64x its FP64 rate.
 //
 // Pull over a symmetric CSR (in-edges == out-edges).  Each iteration is one
-// merge-path SpMV (Merrill & Garland): the n row ends and m edges are merged
-// into n+m items, every thread owns kItems consecutive items, so a hub's row
-// is split across as many threads as it needs.  A CTA first stages its row
-// ends and the gathered contributions contrib[col[j]] of its edge range in
-// shared memory with coalesced loads, then each thread merges sequentially
-// from shared memory.  Rows that end in the thread where they start are
-// finalized directly (rank, next contribution, dangling mass); rows split
-// across threads add their pieces into an FP64 accumulator and are finalized
-// by one fixup thread each.
+// merge-path SpMV (Merrill & Garland): the n row ends and m edges form n+m
+// merge items cut into 1792-item tiles, one CTA per tile, 7 items per thread,
+// so a hub's row spreads over as many threads and CTAs as it needs.  The
+// tile boundaries depend only on the graph and are computed once
+// (merge_tiles).  A CTA stages its row ends and the gathered contributions
+// contrib[col[j]] of its edges in shared memory with coalesced loads, each
+// thread merges its items sequentially, and a segmented warp scan combines
+// the partial sums of rows that span threads.  Rows that start and end in
+// the CTA are finalized in place; a row crossing a CTA boundary adds its
+// pieces to an FP64 accumulator (about two global atomics per tile) and is
+// finalized by one fixup thread.
 #include <algorithm>
 
 #include "ptg_device.cuh"
 
 namespace ptg {
-namespace {
 
 constexpr int kPrItems = 7;
 constexpr int kPrTile = kBlock * kPrItems;
+
+namespace {
+
+struct ff {
+    float hi, lo;
+};
+
+// Knuth's two-sum, renormalized (compensated two-float accumulation).
+__device__ __forceinline__ ff ff_add(ff a, float b) {
+    float s = a.hi + b;
+    float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b - bb);
+    e += a.lo;
+    float h = s + e;
+    return ff{h, e - (h - s)};
+}
+
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+    float s = a.hi + b.hi;
+    float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e += a.lo + b.lo;
+    float h = s + e;
+    return ff{h, e - (h - s)};
+}
+
+__device__ __forceinline__ double ff_dbl(ff a) { return (double)a.hi + (double)a.lo; }
 
 struct PrArgs {
     uint64_t n, m;
     const void *off;          // OffT[n+1]
     const uint32_t *col;
+    const uint64_t *tiles;    // row index at each tile's first merge item
     const float *contrib_in;  // [n]
     float *contrib_out;       // [n]
     float *rank_out;          // [n] or nullptr (written on the last iteration)
-    double *acc;              // [n] zero on entry for split rows; re-zeroed by fixup
-    uint32_t *split_rows;     // rows split across threads
+    double *acc;              // [n] zero on entry; split rows only, re-zeroed by fixup
+    uint32_t *split_rows;     // rows that cross a CTA boundary (listed by their first CTA)
     unsigned *split_count;
     uint32_t split_cap;
     const double *dangling_in;
@@ -62,8 +93,17 @@ __device__ __forceinline__ uint64_t merge_search(const OffT *row_end, uint64_t n
 }
 
 template <class OffT>
-__device__ __forceinline__ double finalize_row(const PrArgs &a, uint64_t v, OffT deg, double sum,
-                                               double dang_in, double &dang_local) {
+__global__ void k_merge_tiles(const OffT *off, uint64_t n, uint64_t m, uint64_t ntiles, uint64_t *tiles) {
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t <= ntiles;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t d = min(t * (uint64_t)kPrTile, n + m);
+        tiles[t] = merge_search(off + 1, n, m, d);
+    }
+}
+
+template <class OffT>
+__device__ __forceinline__ void finalize_row(const PrArgs &a, uint64_t v, OffT deg, double sum,
+                                             double dang_in, double &dang_local) {
     double r;
     if (a.personalized) {
         r = a.d * sum;
@@ -77,95 +117,145 @@ __device__ __forceinline__ double finalize_row(const PrArgs &a, uint64_t v, OffT
         dang_local += (double)rf;
         a.contrib_out[v] = 0.f;
     } else {
-        a.contrib_out[v] = (float)((double)rf / (double)deg);
+        a.contrib_out[v] = rf / (float)deg;
     }
-    return r;
 }
 
 template <class OffT>
 __global__ void __launch_bounds__(kBlock) k_spmv(PrArgs a) {
     __shared__ OffT s_end[kPrTile + 1];   // row ends of the CTA's rows
     __shared__ float s_val[kPrTile + 1];  // gathered contributions of its edges
-    __shared__ uint64_t s_i0, s_j0, s_i1, s_j1;
+    __shared__ uint32_t s_key[kBlock];    // carry row per thread (local index)
+    __shared__ float s_shi[kBlock], s_slo[kBlock];
+    __shared__ uint32_t s_wfirst[kBlock / 32], s_wlast[kBlock / 32];
+    __shared__ float s_whi[kBlock / 32], s_wlo[kBlock / 32];
     const OffT *off = reinterpret_cast<const OffT *>(a.off);
     const OffT *row_end = off + 1;
     const uint64_t n = a.n, m = a.m, total = n + m;
     const double dang_in = *a.dangling_in;
+    const uint32_t NONE = 0xFFFFFFFFu;
     double dang_local = 0.0;
     uint64_t ntiles = (total + kPrTile - 1) / kPrTile;
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         uint64_t d0 = tile * kPrTile, d1 = min(total, d0 + kPrTile);
-        if (threadIdx.x == 0) {
-            uint64_t i0 = merge_search(row_end, n, m, d0);
-            uint64_t i1 = merge_search(row_end, n, m, d1);
-            s_i0 = i0;
-            s_j0 = d0 - i0;
-            s_i1 = i1;
-            s_j1 = d1 - i1;
-        }
-        __syncthreads();
-        uint64_t i0 = s_i0, j0 = s_j0, i1 = s_i1, j1 = s_j1;
+        uint64_t i0 = a.tiles[tile], i1 = a.tiles[tile + 1];
+        uint64_t j0 = d0 - i0, j1 = d1 - i1;
         uint64_t nrows = i1 - i0, nedges = j1 - j0;
-        // stage row ends (one extra so a thread may look at the row it sits in)
         for (uint64_t k = threadIdx.x; k <= nrows; k += kBlock)
             s_end[k] = (i0 + k < n) ? row_end[i0 + k] : (OffT)m;
         for (uint64_t k = threadIdx.x; k < nedges; k += kBlock) s_val[k] = a.contrib_in[a.col[j0 + k]];
         __syncthreads();
-        // this thread's diagonal range inside the tile
+        // this thread's merge items inside the tile
         uint64_t td0 = min((uint64_t)threadIdx.x * kPrItems, nrows + nedges);
         uint64_t td1 = min(td0 + kPrItems, nrows + nedges);
-        // local merge search over the staged row ends
         uint64_t lo = td0 > nedges ? td0 - nedges : 0, hi = min(td0, nrows);
         while (lo < hi) {
             uint64_t mid = (lo + hi) >> 1;
             if ((uint64_t)s_end[mid] - j0 <= td0 - mid - 1) lo = mid + 1;
             else hi = mid;
         }
-        uint64_t li = lo, lj = td0 - lo;  // local row / edge index
-        if (td0 < td1) {
-            uint64_t row = i0 + li;
-            uint64_t j = j0 + lj;
-            OffT rstart = row < n ? off[row] : (OffT)m;
-            bool started_here = (j == (uint64_t)rstart);
-            double sum = 0.0;
-            for (uint64_t k = td0; k < td1; k++) {
-                if (li < nrows && (j0 + lj) >= (uint64_t)s_end[li]) {
-                    // row end item: finalize row i0+li
-                    uint64_t v = i0 + li;
-                    if (started_here) {
-                        OffT deg = s_end[li] - rstart;
-                        finalize_row<OffT>(a, v, deg, sum, dang_in, dang_local);
-                    } else {
-                        atomicAdd(&a.acc[v], sum);
-                    }
-                    sum = 0.0;
-                    li++;
-                    rstart = s_end[li - 1];
-                    started_here = true;
+        uint64_t li = lo, lj = td0 - lo;
+        // the row the thread starts in began before this thread's first edge?
+        uint64_t row_start = (i0 + li == 0) ? 0 : (li == 0 ? (uint64_t)off[i0] : (uint64_t)s_end[li - 1]);
+        bool cont = (j0 + lj) > row_start;  // first row is a continuation
+        uint32_t first_row = NONE;
+        ff first_val{0.f, 0.f};
+        ff sum{0.f, 0.f};
+        for (uint64_t k = td0; k < td1; k++) {
+            if (li < nrows && (j0 + lj) >= (uint64_t)s_end[li]) {
+                uint64_t v = i0 + li;
+                if (cont) {  // combined with earlier threads after the scan
+                    first_row = (uint32_t)li;
+                    first_val = sum;
+                    cont = false;
                 } else {
-                    sum += (double)s_val[lj];
-                    lj++;
+                    OffT deg = s_end[li] - (OffT)row_start;
+                    finalize_row<OffT>(a, v, deg, ff_dbl(sum), dang_in, dang_local);
                 }
+                row_start = s_end[li];
+                sum = ff{0.f, 0.f};
+                li++;
+            } else {
+                sum = ff_add(sum, s_val[lj]);
+                lj++;
             }
-            // carry-out: the current row continues past this thread
-            uint64_t v = i0 + li;
-            if (v < n && (j0 + lj) > (uint64_t)rstart) {
-                atomicAdd(&a.acc[v], sum);
-                if (started_here) {
+        }
+        // carry: the row in progress at the end of this thread's items
+        uint32_t key = (li < nrows || (i0 + li < n && j0 + lj > row_start)) ? (uint32_t)li : NONE;
+        if (td0 >= td1) key = NONE;
+        // segmented inclusive scan of carries by row (warp level)
+        unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+        ff s = key == NONE ? ff{0.f, 0.f} : sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t ok = __shfl_up_sync(0xffffffffu, key, o);
+            float oh = __shfl_up_sync(0xffffffffu, s.hi, o);
+            float ol = __shfl_up_sync(0xffffffffu, s.lo, o);
+            if (lane >= (unsigned)o && ok == key && key != NONE) s = ff_add(s, ff{oh, ol});
+        }
+        uint32_t wfirst = __shfl_sync(0xffffffffu, key, 0);
+        if (lane == 31) {
+            s_wlast[wid] = key;
+            s_whi[wid] = s.hi;
+            s_wlo[wid] = s.lo;
+        }
+        if (lane == 0) s_wfirst[wid] = wfirst;
+        __syncthreads();
+        // carries from earlier warps continuing the same row
+        if (key != NONE && key == wfirst) {
+            for (int w = (int)wid - 1; w >= 0; w--) {
+                if (s_wlast[w] != key) break;
+                s = ff_add(s, ff{s_whi[w], s_wlo[w]});
+                if (s_wfirst[w] != key) break;
+            }
+        }
+        s_key[threadIdx.x] = key;
+        s_shi[threadIdx.x] = s.hi;
+        s_slo[threadIdx.x] = s.lo;
+        __syncthreads();
+        // the first row this thread ended: add the carries of earlier threads
+        if (first_row != NONE) {
+            ff tot = first_val;
+            if (threadIdx.x > 0 && s_key[threadIdx.x - 1] == first_row)
+                tot = ff_add(tot, ff{s_shi[threadIdx.x - 1], s_slo[threadIdx.x - 1]});
+            uint64_t v = i0 + first_row;
+            uint64_t rs = first_row == 0 ? (uint64_t)off[i0] : (uint64_t)s_end[first_row - 1];
+            if (rs < j0) {
+                atomicAdd(&a.acc[v], ff_dbl(tot));  // began in an earlier CTA: fixup finalizes
+            } else {
+                OffT deg = s_end[first_row] - (OffT)rs;
+                finalize_row<OffT>(a, v, deg, ff_dbl(tot), dang_in, dang_local);
+            }
+        }
+        // Row i1 (local index nrows) is the only row that can still be open at
+        // the end of the tile; if it has edges here it continues in a later
+        // CTA.  Its carry is the scan value of the last thread keyed to it.
+        if (threadIdx.x == kBlock - 1 && i1 < n) {
+            uint64_t rs = nrows == 0 ? (uint64_t)off[i0] : (uint64_t)s_end[nrows - 1];
+            if (j1 > rs) {
+                ff tot{0.f, 0.f};
+                for (int t = kBlock - 1; t >= 0; t--) {
+                    if (s_key[t] == (uint32_t)nrows) {
+                        tot = ff{s_shi[t], s_slo[t]};
+                        break;
+                    }
+                }
+                atomicAdd(&a.acc[i1], ff_dbl(tot));
+                if (rs >= j0) {  // it began in this tile: list it once for the fixup
                     unsigned pos = atomicAdd(a.split_count, 1u);
-                    if (pos < a.split_cap) a.split_rows[pos] = (uint32_t)v;
+                    if (pos < a.split_cap) a.split_rows[pos] = (uint32_t)i1;
                 }
             }
         }
         __syncthreads();
     }
-    double s = block_reduce_sum(dang_local);
-    if (threadIdx.x == 0 && s != 0.0) atomicAdd(a.dangling_out, s);
+    double sd = block_reduce_sum(dang_local);
+    if (threadIdx.x == 0 && sd != 0.0) atomicAdd(a.dangling_out, sd);
 }
 
-// Finalize rows that were split across threads (each listed once).
+// Finalize rows that crossed a CTA boundary (each listed once).
 template <class OffT>
-__global__ void k_fixup(PrArgs a) {
+__global__ void __launch_bounds__(kBlock) k_fixup(PrArgs a) {
     const OffT *off = reinterpret_cast<const OffT *>(a.off);
     unsigned cnt = min(*a.split_count, a.split_cap);
     const double dang_in = *a.dangling_in;
@@ -191,7 +281,7 @@ __global__ void __launch_bounds__(kBlock) k_pr_init(const OffT *off, uint64_t n,
             dl += r;
             contrib[v] = 0.f;
         } else {
-            contrib[v] = (float)((double)r / (double)deg);
+            contrib[v] = r / (float)deg;
         }
     }
     double s = block_reduce_sum(dl);
@@ -206,13 +296,12 @@ void pagerank_impl(ptg_graph *g, bool personalized, uint32_t src, double damping
     cudaStream_t st = ctx->stream;
     const uint64_t n = g->n, m = g->m;
     const int sms = ctx->sm_count;
-    uint64_t total = n + m;
-    uint64_t nthreads = (total + kPrItems - 1) / kPrItems;
-    uint32_t split_cap = (uint32_t)std::min<uint64_t>(nthreads + 1, 0xFFFFFFF0ull);
-    // workspace: contrib[2] (float), acc (double), split rows, dangling[2], split count
-    ws.aux.ensure(n * 8 + 64);      // acc
-    ws.aux2.ensure(2 * n * 4 + 64); // contrib ping-pong
-    ws.q[0].ensure((uint64_t)split_cap * 4);
+    uint64_t ntiles = (n + m + kPrTile - 1) / kPrTile;
+    const uint64_t *tiles = merge_tiles(g);
+    uint32_t split_cap = (uint32_t)std::min<uint64_t>(ntiles + 1, 0xFFFFFFF0ull);
+    ws.aux.ensure(n * 8 + 64);       // acc
+    ws.aux2.ensure(2 * n * 4 + 64);  // contrib ping-pong
+    ws.q[0].ensure(std::max<uint64_t>((uint64_t)split_cap * 4, n * 4));
     ws.bsum.ensure(1024 * 8);
     double *acc = ws.aux.as<double>();
     float *contrib[2] = {ws.aux2.as<float>(), ws.aux2.as<float>() + n};
@@ -224,7 +313,7 @@ void pagerank_impl(ptg_graph *g, bool personalized, uint32_t src, double damping
     const OffT *off = g->d_off.as<OffT>();
     launch(ctx, "k_pr_init", k_pr_init<OffT>, fill_grid, kBlock, 0, st, off, n, personalized ? 1 : 0, src,
            contrib[0], &dang[0]);
-    int grid = grid_for(total, kPrTile, sms * 8);
+    int grid = grid_for(ntiles, 1, sms * 8);
     for (uint32_t it = 0; it < iters; it++) {
         int cin = it & 1, cout = cin ^ 1;
         PTG_CUDA_TRY(cudaMemsetAsync(&dang[cout], 0, 8, st));
@@ -234,6 +323,7 @@ void pagerank_impl(ptg_graph *g, bool personalized, uint32_t src, double damping
         a.m = m;
         a.off = off;
         a.col = g->d_col.as<uint32_t>();
+        a.tiles = tiles;
         a.contrib_in = contrib[cin];
         a.contrib_out = contrib[cout];
         a.rank_out = (it + 1 == iters) ? d_rank : nullptr;
@@ -247,18 +337,35 @@ void pagerank_impl(ptg_graph *g, bool personalized, uint32_t src, double damping
         a.personalized = personalized ? 1 : 0;
         a.src = src;
         launch(ctx, "k_spmv", k_spmv<OffT>, grid, kBlock, 0, st, a);
-        launch(ctx, "k_fixup", k_fixup<OffT>, sms * 4, kBlock, 0, st, a);
+        launch(ctx, "k_fixup", k_fixup<OffT>, sms * 2, kBlock, 0, st, a);
         PTG_CUDA_TRY(cudaGetLastError());
         rr.edges_relaxed += m;
-    }
-    if (iters == 0) {
-        // rank = r0
-        PTG_CUDA_TRY(cudaMemsetAsync(d_rank, 0, n * 4, st));
     }
     rr.iterations = iters;
 }
 
+template <class OffT>
+void build_merge_tiles(ptg_graph *g) {
+    uint64_t ntiles = (g->n + g->m + kPrTile - 1) / kPrTile;
+    g->d_tiles.ensure((ntiles + 1) * 8);
+    launch(g->ctx, "k_merge_tiles", k_merge_tiles<OffT>, grid_for(ntiles + 1, kBlock, g->ctx->sm_count * 8),
+           kBlock, 0, g->ctx->stream, g->d_off.as<OffT>(), g->n, g->m, ntiles, g->d_tiles.as<uint64_t>());
+    PTG_CUDA_TRY(cudaGetLastError());
+}
+
 }  // namespace
+
+// Merge-path tile table of the resident graph (row index at each 1792-item
+// tile start), built on first use and kept with the graph.
+const uint64_t *merge_tiles(ptg_graph *g) {
+    if (!g->d_tiles.p) {
+        if (g->off64) build_merge_tiles<unsigned long long>(g);
+        else build_merge_tiles<uint32_t>(g);
+    }
+    return g->d_tiles.as<uint64_t>();
+}
+
+int merge_tile_items() { return kPrTile; }
 
 void run_pagerank(ptg_graph *g, bool personalized, uint32_t src, double damping, uint32_t iters,
                   float *d_rank, RunResult &rr) {

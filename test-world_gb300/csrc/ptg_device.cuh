@@ -105,6 +105,23 @@ __device__ __forceinline__ uint64_t last_le(const T *a, uint64_t lo, uint64_t hi
     return lo;
 }
 
+// Block-cooperative version of last_le (all kBlock threads call it): each
+// round probes kBlock evenly spaced positions at once, so a search over 2^24
+// entries takes 3 rounds of parallel loads instead of 24 dependent ones.
+template <class T, class K>
+__device__ __forceinline__ uint64_t block_last_le(const T *a, uint64_t lo, uint64_t hi, K key) {
+    while (hi - lo > 1) {
+        uint64_t step = (hi - lo + kBlock - 1) / kBlock;
+        uint64_t pos = lo + (uint64_t)threadIdx.x * step;
+        bool le = threadIdx.x == 0 || (pos < hi && (uint64_t)a[pos] <= (uint64_t)key);
+        int cnt = __syncthreads_count(le);
+        uint64_t nlo = lo + (uint64_t)(cnt - 1) * step;
+        hi = min(hi, nlo + step);
+        lo = nlo;
+    }
+    return lo;
+}
+
 __device__ __forceinline__ bool bit_test(const uint32_t *bm, uint32_t v) {
     return (bm[v >> 5] >> (v & 31u)) & 1u;
 }

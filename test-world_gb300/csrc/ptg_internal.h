@@ -202,7 +202,7 @@ struct Prof {
 // context / graph
 // --------------------------------------------------------------------------
 struct Workspace {
-    DevBuf value, q[2], bm[2], farq[2], farbm, scan, rowstart, bsum, ctl, aux, aux2, flags;
+    DevBuf value, q[2], bm[2], farq[2], farbm, scan, rowstart, tiles, bsum, ctl, aux, aux2, flags;
     PinnedBuf h_ctl, h_flags;
 };
 
@@ -229,6 +229,7 @@ struct ptg_graph {
     bool symmetric = false, weighted = false, off64 = false;
     // device copies
     ptg::DevBuf d_off, d_col, d_w, d_invdeg;
+    ptg::DevBuf d_tiles;  // merge-path tile table (PageRank, CC), built on first use
     // out-of-core
     bool out_of_core = false;
     uint64_t resident_edges = 0;
@@ -279,5 +280,9 @@ void run_msbfs(ptg_graph *g, const uint32_t *sources, uint32_t k, uint32_t *out,
 void run_cc_batch(ptg_ctx *ctx, uint32_t num_graphs, const uint64_t *vtx_begin,
                   const uint64_t *offsets, const uint32_t *col, uint32_t *labels, RunResult &rr);
 int sm_count_of(ptg_ctx *ctx);
+// Merge-path tiling of a resident graph's n row ends + m edges into tiles of
+// merge_tile_items() items; entry t is the row index at tile t's first item.
+const uint64_t *merge_tiles(ptg_graph *g);
+int merge_tile_items();
 
 }  // namespace ptg

@@ -177,32 +177,35 @@ __device__ __forceinline__ void relax(const PushTargets &t, uint32_t v, uint32_t
     }
 }
 
+// First frontier row of every 2048-edge expand tile (one thread per tile, so
+// the searches run in parallel instead of inside the expanding CTAs).
+template <class OffT>
+__global__ void k_tile_rows(const OffT *sc, const TravCtl *ctl, uint32_t *tr) {
+    uint64_t F = ctl->F, E = ctl->E;
+    uint64_t ntiles = (E + kTile - 1) / kTile;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t <= ntiles;
+         t += (uint64_t)gridDim.x * blockDim.x)
+        tr[t] = (uint32_t)last_le(sc, 0, F, min(t * (uint64_t)kTile, E));
+}
+
 // Load-balanced top-down expansion of the frontier's (resident) edges.
 // mode: 0 BFS (+1), 1 SSSP (+w), 2 CC (propagate value).
 template <class OffT, int MODE>
 __global__ void __launch_bounds__(kBlock) k_expand(const uint32_t *q, const OffT *sc, const OffT *rs,
-                                                   const uint32_t *col, const uint32_t *w,
-                                                   PushTargets t) {
-    __shared__ OffT s_sc[kTile + 1];
-    __shared__ OffT s_rs[kTile + 1];
-    __shared__ uint32_t s_val[kTile + 1];
-    __shared__ uint64_t s_r0, s_nrows;
+                                                   const uint32_t *tr, const uint32_t *col,
+                                                   const uint32_t *w, PushTargets t) {
+    __shared__ OffT s_sc[kTile + 2];
+    __shared__ OffT s_rs[kTile + 2];
+    __shared__ uint32_t s_val[kTile + 2];
     const TravCtl *ctl = t.ctl;
-    uint64_t F = ctl->F;
     uint64_t E = ctl->E;
     uint32_t thr = ctl->threshold;
     uint64_t ntiles = (E + kTile - 1) / kTile;
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         uint64_t t0 = tile * kTile, t1 = min(E, t0 + kTile);
-        if (threadIdx.x == 0) {
-            uint64_t r0 = last_le(sc, 0, F, t0);
-            uint64_t r1 = last_le(sc, r0, F, t1 - 1);
-            s_r0 = r0;
-            s_nrows = r1 - r0 + 1;
-        }
-        __syncthreads();
-        uint64_t r0 = s_r0, nrows = s_nrows;
-        bool staged = nrows <= (uint64_t)kTile;
+        // rows r0..r1 cover the tile (r1 may start exactly at t1: one spare row)
+        uint64_t r0 = tr[tile], nrows = (uint64_t)tr[tile + 1] - r0 + 1;
+        bool staged = nrows <= (uint64_t)kTile + 1;
         if (staged) {
             for (uint64_t k = threadIdx.x; k < nrows; k += kBlock) {
                 s_sc[k] = sc[r0 + k];
@@ -301,20 +304,14 @@ __global__ void __launch_bounds__(kBlock) k_relax_partition(uint64_t e_begin, ui
                                                             const uint32_t *bm_cur, PushTargets t) {
     __shared__ OffT s_off[kTile + 2];
     __shared__ uint32_t s_val[kTile + 1];
-    __shared__ uint64_t s_r0, s_nrows;
     uint32_t thr = t.ctl->threshold;
     uint64_t E = e_end - e_begin;
     uint64_t ntiles = (E + kTile - 1) / kTile;
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         uint64_t t0 = e_begin + tile * kTile, t1 = min(e_end, t0 + kTile);
-        if (threadIdx.x == 0) {
-            uint64_t r0 = last_le(off, v_first, v_last + 1, t0);
-            uint64_t r1 = last_le(off, r0, v_last + 1, t1 - 1);
-            s_r0 = r0;
-            s_nrows = r1 - r0 + 1;
-        }
-        __syncthreads();
-        uint64_t r0 = s_r0, nrows = s_nrows;
+        uint64_t r0 = block_last_le(off, v_first, v_last + 1, t0);
+        uint64_t r1 = block_last_le(off, r0, v_last + 1, t1 - 1);
+        uint64_t nrows = r1 - r0 + 1;
         bool staged = nrows <= (uint64_t)kTile;
         if (staged) {
             for (uint64_t k = threadIdx.x; k < nrows; k += kBlock) {
@@ -401,6 +398,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
     ws.bm[1].ensure(words * 4);
     ws.scan.ensure((n + 1) * sizeof(OffT));
     ws.rowstart.ensure((n + 1) * sizeof(OffT));
+    ws.tiles.ensure((g->resident_edges / kTile + 4) * sizeof(uint32_t));
     const int kScanBlocks = 1024;
     ws.bsum.ensure(kScanBlocks * 8);
     ws.ctl.ensure(sizeof(TravCtl));
@@ -538,12 +536,15 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
                    clip, bsum, sc, rs);
             int eg = sms * 8;
             if (allow_bu) eg = grid_for(E, kTile, sms * 8);
+            uint32_t *tr = ws.tiles.as<uint32_t>();
+            launch(ctx, "k_tile_rows", k_tile_rows<OffT>, allow_bu ? grid_for(E / kTile + 1, kBlock, sms * 4) : sms * 4,
+                   kBlock, 0, st, sc, d_ctl, tr);
             if (kind == TRAV_BFS)
-                launch(ctx, "k_expand_bfs", k_expand<OffT, 0>, eg, kBlock, 0, st, q_cur, sc, rs, col, wt, pt);
+                launch(ctx, "k_expand_bfs", k_expand<OffT, 0>, eg, kBlock, 0, st, q_cur, sc, rs, tr, col, wt, pt);
             else if (kind == TRAV_SSSP)
-                launch(ctx, "k_expand_sssp", k_expand<OffT, 1>, eg, kBlock, 0, st, q_cur, sc, rs, col, wt, pt);
+                launch(ctx, "k_expand_sssp", k_expand<OffT, 1>, eg, kBlock, 0, st, q_cur, sc, rs, tr, col, wt, pt);
             else
-                launch(ctx, "k_expand_cc", k_expand<OffT, 2>, eg, kBlock, 0, st, q_cur, sc, rs, col, wt, pt);
+                launch(ctx, "k_expand_cc", k_expand<OffT, 2>, eg, kBlock, 0, st, q_cur, sc, rs, tr, col, wt, pt);
             PTG_CUDA_TRY(cudaGetLastError());
             if (g->out_of_core) {
                 // stream the active partitions past the resident prefix
