@@ -46,7 +46,25 @@ def parse():
     p.add_argument("--sssp-sources", type=int, default=4)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--profile-case", action="store_true",
+                   help="run one SSSP, one 20-iteration PageRank and one BFS (in that order) on the "
+                        "workload graph and exit: the small fixed case ncu captures run on")
     return p.parse_args()
+
+
+def profile_case(args):
+    import ptgraph
+    ctx = ptgraph.Ctx(int(os.environ.get("LOCAL_RANK", "0")))
+    off, col, w, deg, sources, _ = make_workload(args)
+    G = ctx.graph(off.astype(np.uint32), col, w, symmetric=True)
+    out = {}
+    for name, fn in (("sssp", lambda st: G.sssp(int(sources[0]), stats=st)),
+                     ("pagerank", lambda st: G.pagerank(stats=st)),
+                     ("bfs", lambda st: G.bfs(int(sources[0]), stats=st))):
+        st = {}
+        fn(st)
+        out[name] = {"device_ms": st["device_ms"], "iterations": st["iterations"]}
+    print(json.dumps({"profile_case": out, "n": off.size - 1, "m": col.size}))
 
 
 def dist_init(args):
@@ -197,6 +215,9 @@ def main():
     rank, world, local, pg = dist_init(args)
     if args.impl == "reference":
         run_reference(args, rank, pg)
+        return
+    if args.profile_case:
+        profile_case(args)
         return
     import torch
     import ptgraph
