@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(kBlock) k_hook_tiles(const OffT *off, const ui
         __syncthreads();
         for (uint64_t j = j0 + threadIdx.x; j < j1; j += kBlock) {
             uint64_t u = i0 + last_le(s_start, 0, nrows + 1, j);
-            uint32_t v = col[j];
+            uint32_t v = __ldcs(col + j);
             if (v < u) hook(parent, (uint32_t)u, v);
         }
         __syncthreads();

@@ -101,20 +101,47 @@ __global__ void k_merge_tiles(const OffT *off, uint64_t n, uint64_t m, uint64_t 
     }
 }
 
+// Two-float product (fma gives the exact rounding error of hi*hi).
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+    float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    float h = p + e;
+    return ff{h, e - (h - p)};
+}
+
+__device__ __forceinline__ ff ff_of(double x) {
+    float h = (float)x;
+    return ff{h, (float)(x - (double)h)};
+}
+
+// Per-iteration constants of the update, as two-floats (computed once per CTA
+// in FP64 from the previous iteration's dangling mass):
+//   PR : r = base + d * sum,   base = (1-d)/n + d * dangling / n
+//   PPR: r = d * sum (+ bonus at src), bonus = (1-d) + d * dangling
+struct PrConst {
+    ff base, d, bonus;
+};
+
+__device__ __forceinline__ PrConst pr_const(const PrArgs &a) {
+    double dang = *a.dangling_in;
+    PrConst c;
+    c.d = ff_of(a.d);
+    c.base = a.personalized ? ff{0.f, 0.f} : ff_of((1.0 - a.d) / (double)a.n + a.d * dang / (double)a.n);
+    c.bonus = a.personalized ? ff_of((1.0 - a.d) + a.d * dang) : ff{0.f, 0.f};
+    return c;
+}
+
 template <class OffT>
-__device__ __forceinline__ void finalize_row(const PrArgs &a, uint64_t v, OffT deg, double sum,
-                                             double dang_in, double &dang_local) {
-    double r;
-    if (a.personalized) {
-        r = a.d * sum;
-        if (v == a.src) r += (1.0 - a.d) + a.d * dang_in;
-    } else {
-        r = (1.0 - a.d) / (double)a.n + a.d * (sum + dang_in / (double)a.n);
-    }
-    float rf = (float)r;
+__device__ __forceinline__ void finalize_row(const PrArgs &a, const PrConst &c, uint64_t v, OffT deg,
+                                             ff sum, ff &dang_local) {
+    ff r = ff_add(c.base, ff_mul(c.d, sum));
+    if (a.personalized && v == a.src) r = ff_add(r, c.bonus);
+    float rf = r.hi + r.lo;
     if (a.rank_out) a.rank_out[v] = rf;
     if (deg == 0) {
-        dang_local += (double)rf;
+        dang_local = ff_add(dang_local, rf);
         a.contrib_out[v] = 0.f;
     } else {
         a.contrib_out[v] = rf / (float)deg;
@@ -132,47 +159,49 @@ __global__ void __launch_bounds__(kBlock) k_spmv(PrArgs a) {
     const OffT *off = reinterpret_cast<const OffT *>(a.off);
     const OffT *row_end = off + 1;
     const uint64_t n = a.n, m = a.m, total = n + m;
-    const double dang_in = *a.dangling_in;
+    const PrConst c = pr_const(a);
     const uint32_t NONE = 0xFFFFFFFFu;
-    double dang_local = 0.0;
+    ff dang_local{0.f, 0.f};
     uint64_t ntiles = (total + kPrTile - 1) / kPrTile;
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         uint64_t d0 = tile * kPrTile, d1 = min(total, d0 + kPrTile);
         uint64_t i0 = a.tiles[tile], i1 = a.tiles[tile + 1];
         uint64_t j0 = d0 - i0, j1 = d1 - i1;
-        uint64_t nrows = i1 - i0, nedges = j1 - j0;
-        for (uint64_t k = threadIdx.x; k <= nrows; k += kBlock)
+        // tile-local counts and positions fit 32 bits (at most kPrTile items)
+        uint32_t nrows = (uint32_t)(i1 - i0), nedges = (uint32_t)(j1 - j0);
+        for (uint32_t k = threadIdx.x; k <= nrows; k += kBlock)
             s_end[k] = (i0 + k < n) ? row_end[i0 + k] : (OffT)m;
-        for (uint64_t k = threadIdx.x; k < nedges; k += kBlock) s_val[k] = a.contrib_in[a.col[j0 + k]];
+        for (uint32_t k = threadIdx.x; k < nedges; k += kBlock) s_val[k] = a.contrib_in[__ldcs(a.col + j0 + k)];
         __syncthreads();
-        // this thread's merge items inside the tile
-        uint64_t td0 = min((uint64_t)threadIdx.x * kPrItems, nrows + nedges);
-        uint64_t td1 = min(td0 + kPrItems, nrows + nedges);
-        uint64_t lo = td0 > nedges ? td0 - nedges : 0, hi = min(td0, nrows);
+        // this thread's merge items inside the tile; edge positions are local
+        // (edge j0 + x is x), row ends are converted on the fly
+        uint32_t items = nrows + nedges;
+        uint32_t td0 = min((uint32_t)threadIdx.x * kPrItems, items);
+        uint32_t td1 = min(td0 + kPrItems, items);
+        uint32_t lo = td0 > nedges ? td0 - nedges : 0, hi = min(td0, nrows);
         while (lo < hi) {
-            uint64_t mid = (lo + hi) >> 1;
-            if ((uint64_t)s_end[mid] - j0 <= td0 - mid - 1) lo = mid + 1;
+            uint32_t mid = (lo + hi) >> 1;
+            if ((uint32_t)(s_end[mid] - (OffT)j0) <= td0 - mid - 1) lo = mid + 1;
             else hi = mid;
         }
-        uint64_t li = lo, lj = td0 - lo;
-        // the row the thread starts in began before this thread's first edge?
-        uint64_t row_start = (i0 + li == 0) ? 0 : (li == 0 ? (uint64_t)off[i0] : (uint64_t)s_end[li - 1]);
-        bool cont = (j0 + lj) > row_start;  // first row is a continuation
+        uint32_t li = lo, lj = td0 - lo;
+        // local start of the row the thread starts in (may be before the tile)
+        int64_t row_start = (li == 0) ? (int64_t)off[i0] - (int64_t)j0 : (int64_t)(s_end[li - 1] - (OffT)j0);
+        bool cont = (int64_t)lj > row_start;  // first row is a continuation
         uint32_t first_row = NONE;
         ff first_val{0.f, 0.f};
         ff sum{0.f, 0.f};
-        for (uint64_t k = td0; k < td1; k++) {
-            if (li < nrows && (j0 + lj) >= (uint64_t)s_end[li]) {
-                uint64_t v = i0 + li;
+        for (uint32_t k = td0; k < td1; k++) {
+            uint32_t end_l = li < nrows ? (uint32_t)(s_end[li] - (OffT)j0) : 0xFFFFFFFFu;
+            if (lj >= end_l) {
                 if (cont) {  // combined with earlier threads after the scan
-                    first_row = (uint32_t)li;
+                    first_row = li;
                     first_val = sum;
                     cont = false;
                 } else {
-                    OffT deg = s_end[li] - (OffT)row_start;
-                    finalize_row<OffT>(a, v, deg, ff_dbl(sum), dang_in, dang_local);
+                    finalize_row<OffT>(a, c, i0 + li, (OffT)(end_l - row_start), sum, dang_local);
                 }
-                row_start = s_end[li];
+                row_start = end_l;
                 sum = ff{0.f, 0.f};
                 li++;
             } else {
@@ -181,7 +210,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv(PrArgs a) {
             }
         }
         // carry: the row in progress at the end of this thread's items
-        uint32_t key = (li < nrows || (i0 + li < n && j0 + lj > row_start)) ? (uint32_t)li : NONE;
+        uint32_t key = (li < nrows || (i0 + li < n && (int64_t)lj > row_start)) ? li : NONE;
         if (td0 >= td1) key = NONE;
         // segmented inclusive scan of carries by row (warp level)
         unsigned lane = lane_id(), wid = threadIdx.x >> 5;
@@ -224,7 +253,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv(PrArgs a) {
                 atomicAdd(&a.acc[v], ff_dbl(tot));  // began in an earlier CTA: fixup finalizes
             } else {
                 OffT deg = s_end[first_row] - (OffT)rs;
-                finalize_row<OffT>(a, v, deg, ff_dbl(tot), dang_in, dang_local);
+                finalize_row<OffT>(a, c, v, deg, tot, dang_local);
             }
         }
         // Row i1 (local index nrows) is the only row that can still be open at
@@ -249,22 +278,23 @@ __global__ void __launch_bounds__(kBlock) k_spmv(PrArgs a) {
         }
         __syncthreads();
     }
-    double sd = block_reduce_sum(dang_local);
+    double sd = block_reduce_sum(ff_dbl(dang_local));
     if (threadIdx.x == 0 && sd != 0.0) atomicAdd(a.dangling_out, sd);
 }
 
-// Finalize rows that crossed a CTA boundary (each listed once).
+// Finalize rows that crossed a CTA boundary (each listed once; split rows
+// have edges, so none of them adds dangling mass).
 template <class OffT>
 __global__ void __launch_bounds__(kBlock) k_fixup(PrArgs a) {
     const OffT *off = reinterpret_cast<const OffT *>(a.off);
     unsigned cnt = min(*a.split_count, a.split_cap);
-    const double dang_in = *a.dangling_in;
-    double dl = 0.0;
+    const PrConst c = pr_const(a);
+    ff dl{0.f, 0.f};
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
         uint32_t v = a.split_rows[i];
         double s = a.acc[v];
         a.acc[v] = 0.0;
-        finalize_row<OffT>(a, v, off[v + 1] - off[v], s, dang_in, dl);
+        finalize_row<OffT>(a, c, v, off[v + 1] - off[v], ff_of(s), dl);
     }
 }
 

@@ -202,7 +202,7 @@ struct Prof {
 // context / graph
 // --------------------------------------------------------------------------
 struct Workspace {
-    DevBuf value, q[2], bm[2], farq[2], farbm, scan, rowstart, tiles, bsum, ctl, aux, aux2, flags;
+    DevBuf value, q[2], bm[2], farq[2], farbm, vis, scan, rowstart, tiles, bsum, ctl, aux, aux2, flags;
     PinnedBuf h_ctl, h_flags;
 };
 
@@ -230,6 +230,7 @@ struct ptg_graph {
     // device copies
     ptg::DevBuf d_off, d_col, d_w, d_invdeg;
     ptg::DevBuf d_tiles;  // merge-path tile table (PageRank, CC), built on first use
+    ptg::DevBuf d_nzbm;   // bitmap of vertices with edges (bottom-up BFS), built on first use
     // out-of-core
     bool out_of_core = false;
     uint64_t resident_edges = 0;

@@ -68,10 +68,11 @@ __global__ void k_fill_bits(uint32_t *bm, uint64_t n) {
 
 // Seed a single-source frontier.
 __global__ void k_seed(uint32_t *value, uint32_t src, uint32_t base, uint32_t *q, uint32_t *bm,
-                       TravCtl *ctl) {
+                       uint32_t *vis, TravCtl *ctl) {
     value[src] = base;
     q[0] = src;
     bm[src >> 5] |= 1u << (src & 31u);
+    if (vis) vis[src >> 5] |= 1u << (src & 31u);
     ctl->F = 1;
 }
 
@@ -152,7 +153,21 @@ struct PushTargets {
     uint32_t *far_bm;
     TravCtl *ctl;
     uint32_t cap;      // queue capacity (n)
+    uint32_t *vis;     // BFS: visited bitmap (nullptr otherwise)
 };
+
+// BFS relax: every target of a level gets the same value, so the first claim
+// of the visited bit decides (a 2 MB bitmap stays in L2, the level array does
+// not); the level is a plain store.
+__device__ __forceinline__ void relax_bfs(const PushTargets &t, uint32_t v, uint32_t nd) {
+    uint32_t bit = 1u << (v & 31u);
+    if (t.vis[v >> 5] & bit) return;
+    uint32_t prev = atomicOr(&t.vis[v >> 5], bit);
+    if (prev & bit) return;
+    t.value[v] = nd;
+    atomicOr(&t.bm_next[v >> 5], bit);
+    warp_append(t.q_next, &t.ctl->next_tail, t.cap, &t.ctl->error, v);
+}
 
 // Relax one edge: the reference's rule (gpu_kernels.cu:126-131), plus the
 // near/far routing and bitmap dedup of the next frontier.
@@ -231,44 +246,101 @@ __global__ void __launch_bounds__(kBlock) k_expand(const uint32_t *q, const OffT
                 uval = t.value[q[row]];
             }
             uint64_t e = (uint64_t)rsv + (j - (uint64_t)scv);
-            uint32_t v = col[e];
-            uint32_t nd = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + w[e] : uval);
-            relax(t, v, nd, thr);
+            uint32_t v = __ldcs(col + e);
+            if (MODE == 0 && t.vis) {
+                relax_bfs(t, v, uval + 1u);
+            } else {
+                uint32_t nd = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + __ldcs(w + e) : uval);
+                relax(t, v, nd, thr);
+            }
         }
         __syncthreads();
     }
 }
 
-// Bottom-up BFS round (symmetric graphs): each unvisited vertex scans its
-// neighbours for one in the current frontier bitmap.  A warp owns 32
-// consecutive vertices, so it writes its word of the next bitmap with one
-// store (ballot) and appends its discoveries with one atomic.
+// Bitmap of vertices with at least one edge (bottom-up BFS never looks at the
+// others: on a symmetric graph they are unreachable).
+template <class OffT>
+__global__ void k_nonzero_bits(const OffT *off, uint64_t n, uint32_t *nz) {
+    uint64_t words = (n + 31) / 32;
+    for (uint64_t wd = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; wd < words;
+         wd += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t bits = 0;
+        for (int b = 0; b < 32; b++) {
+            uint64_t v = wd * 32 + b;
+            if (v < n && off[v + 1] > off[v]) bits |= 1u << b;
+        }
+        nz[wd] = bits;
+    }
+}
+
+// Bottom-up BFS round (symmetric graphs): each unvisited vertex with edges
+// looks for a neighbour in the current frontier bitmap.  A warp takes 1024
+// consecutive vertices (32 bitmap words): it compacts the candidates
+// (non-zero degree, not yet visited) into a shared list so all lanes stay
+// busy, checks neighbours four at a time (four independent load chains per
+// step instead of one), and writes its 32 words of the next-frontier and
+// visited bitmaps with plain stores.
+constexpr int kBuWarps = kBlock / 32;
 template <class OffT>
 __global__ void __launch_bounds__(kBlock) k_bottom_up(uint64_t n, const OffT *off,
                                                       const uint32_t *col, const uint32_t *bm_cur,
-                                                      PushTargets t) {
-    uint32_t newval = t.ctl->level_val + 1u;
-    uint64_t nwarps_total = (uint64_t)gridDim.x * (kBlock / 32);
-    uint64_t wglobal = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5);
-    uint64_t words = (n + 31) / 32;
-    for (uint64_t wd = wglobal; wd < words; wd += nwarps_total) {
-        uint64_t v = wd * 32 + lane_id();
-        bool found = false;
-        if (v < n && t.value[v] == PTG_UNREACHED) {
+                                                      const uint32_t *nz, PushTargets t) {
+    __shared__ uint32_t s_list[kBuWarps][1024];
+    __shared__ uint32_t s_found[kBuWarps][32];
+    const uint32_t newval = t.ctl->level_val + 1u;
+    const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+    const uint64_t words = (n + 31) / 32;
+    const uint64_t chunks = (words + 31) / 32;
+    const uint64_t nwarps_total = (uint64_t)gridDim.x * kBuWarps;
+    for (uint64_t c = (uint64_t)blockIdx.x * kBuWarps + wid; c < chunks; c += nwarps_total) {
+        uint64_t wd = c * 32 + lane;
+        uint32_t visw = 0, cand = 0;
+        if (wd < words) {
+            visw = t.vis[wd];
+            cand = nz[wd] & ~visw;
+        }
+        // compact candidate vertex ids of the 32 words into s_list[wid]
+        uint32_t cnt = __popc(cand), pre = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, pre, o);
+            if (lane >= (unsigned)o) pre += y;
+        }
+        uint32_t total = __shfl_sync(0xffffffffu, pre, 31);
+        uint32_t pos = pre - cnt;
+        while (cand) {
+            int b = __ffs(cand) - 1;
+            cand &= cand - 1;
+            s_list[wid][pos++] = (uint32_t)(wd * 32 + b);
+        }
+        s_found[wid][lane] = 0;
+        __syncwarp();
+        for (uint32_t i = lane; i < total; i += 32) {
+            uint32_t v = s_list[wid][i];
             OffT b = off[v], e = off[v + 1];
-            for (OffT k = b; k < e; k++) {
-                if (bit_test(bm_cur, col[k])) {
-                    found = true;
-                    break;
-                }
+            bool found = false;
+            for (OffT k = b; k < e && !found; k += 4) {
+                uint32_t c0 = col[k];
+                uint32_t c1 = k + 1 < e ? col[k + 1] : c0;
+                uint32_t c2 = k + 2 < e ? col[k + 2] : c0;
+                uint32_t c3 = k + 3 < e ? col[k + 3] : c0;
+                found = bit_test(bm_cur, c0) | bit_test(bm_cur, c1) | bit_test(bm_cur, c2) |
+                        bit_test(bm_cur, c3);
+            }
+            if (found) {
+                atomicOr(&s_found[wid][(v >> 5) - (uint32_t)(c * 32)], 1u << (v & 31u));
+                t.value[v] = newval;
+                warp_append(t.q_next, &t.ctl->next_tail, t.cap, &t.ctl->error, v);
             }
         }
-        unsigned ballot = __ballot_sync(0xffffffffu, found);
-        if (lane_id() == 0 && ballot) t.bm_next[wd] = ballot;
-        if (found) {
-            t.value[v] = newval;
-            warp_append(t.q_next, &t.ctl->next_tail, t.cap, &t.ctl->error, (uint32_t)v);
+        __syncwarp();
+        if (wd < words) {
+            uint32_t f = s_found[wid][lane];
+            t.bm_next[wd] = f;
+            if (f) t.vis[wd] = visw | f;
         }
+        __syncwarp();
     }
 }
 
@@ -333,8 +405,8 @@ __global__ void __launch_bounds__(kBlock) k_relax_partition(uint64_t e_begin, ui
             }
             if (uval == PTG_UNREACHED) continue;
             uint64_t le = j - e_begin;
-            uint32_t v = stage_col[le];
-            uint32_t nd = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + stage_w[le] : uval);
+            uint32_t v = __ldcs(stage_col + le);
+            uint32_t nd = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + __ldcs(stage_w + le) : uval);
             relax(t, v, nd, thr);
         }
         __syncthreads();
@@ -440,14 +512,27 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
             PTG_CUDA_TRY(cudaMemsetAsync(ws.farbm.p, 0, words * 4, st));
         }
     }
+    // BFS on a resident graph claims vertices through a visited bitmap
+    bool use_vis = kind == TRAV_BFS && !g->out_of_core;
+    uint32_t *vis = nullptr;
+    if (use_vis) {
+        ws.vis.ensure(words * 4);
+        vis = ws.vis.as<uint32_t>();
+        PTG_CUDA_TRY(cudaMemsetAsync(vis, 0, words * 4, st));
+    }
     PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &init, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
     if (kind != TRAV_CCPROP)
         launch(ctx, "k_seed", k_seed, 1, 1, 0, st, d_value, src, base, ws.q[0].as<uint32_t>(),
-               ws.bm[0].as<uint32_t>(), d_ctl);
+               ws.bm[0].as<uint32_t>(), vis, d_ctl);
     PTG_CUDA_TRY(cudaGetLastError());
 
     bool allow_bu = kind == TRAV_BFS && g->symmetric && !g->out_of_core &&
                     !(flags & (PTG_NO_DIRECTION_OPT | PTG_REFERENCE_SCHEDULE));
+    if (allow_bu && !g->d_nzbm.p) {
+        g->d_nzbm.ensure(words * 4);
+        launch(ctx, "k_nonzero_bits", k_nonzero_bits<OffT>, grid_for(words, kBlock, sms * 8), kBlock, 0, st, off,
+               n, g->d_nzbm.as<uint32_t>());
+    }
     int cur = 0, far_cur = 0;
     uint64_t F = init.F, far_count = 0, m_unvisited = g->m;
     uint32_t threshold = init.threshold, level_val = base;
@@ -506,7 +591,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         uint32_t *bm_cur = ws.bm[cur].as<uint32_t>(), *bm_nxt = ws.bm[cur ^ 1].as<uint32_t>();
         PTG_CUDA_TRY(cudaMemsetAsync(bm_nxt, 0, words * 4, st));
         PushTargets pt{d_value, q_nxt, bm_nxt, use_far ? ws.farq[far_cur].as<uint32_t>() : nullptr,
-                       use_far ? ws.farbm.as<uint32_t>() : nullptr, d_ctl, (uint32_t)n};
+                       use_far ? ws.farbm.as<uint32_t>() : nullptr, d_ctl, (uint32_t)n, vis};
         int scan_blocks = grid_for(F, kBlock, kScanBlocks);
         unsigned long long *bsum = ws.bsum.as<unsigned long long>();
         OffT *sc = ws.scan.as<OffT>(), *rs = ws.rowstart.as<OffT>();
@@ -529,8 +614,8 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
             if (h_ctl->level_val != level_val) {
                 PTG_CUDA_TRY(cudaMemcpyAsync(&d_ctl->level_val, &level_val, 4, cudaMemcpyHostToDevice, st));
             }
-            launch(ctx, "k_bottom_up", k_bottom_up<OffT>, grid_for(words * 32, kBlock, sms * 16), kBlock, 0,
-                   st, n, off, col, bm_cur, pt);
+            launch(ctx, "k_bottom_up", k_bottom_up<OffT>, grid_for((words + 31) / 32, kBuWarps, sms * 6),
+                   kBlock, 0, st, n, off, col, bm_cur, (const uint32_t *)g->d_nzbm.as<uint32_t>(), pt);
         } else {
             launch(ctx, "k_scan_write", k_scan_write<OffT>, scan_blocks, kBlock, 0, st, q_cur, d_ctl, off,
                    clip, bsum, sc, rs);
