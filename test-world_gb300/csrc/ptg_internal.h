@@ -122,7 +122,8 @@ struct TravCtl {
     unsigned int dir;             // 0 top-down, 1 bottom-up
     unsigned int level_val;       // BFS: value of current frontier vertices
     unsigned int error;           // nonzero: a kernel detected a bad index
-    unsigned int pad[4];
+    unsigned int bu_next;         // bottom-up BFS chunk counter (zero before each round)
+    unsigned int pad[3];
 };
 
 // --------------------------------------------------------------------------

@@ -192,6 +192,33 @@ __device__ __forceinline__ void relax(const PushTargets &t, uint32_t v, uint32_t
     }
 }
 
+// Small frontiers (most rounds): one CTA does the work of k_scan_reduce,
+// k_scan_bsums and k_scan_write in a single launch.
+constexpr uint32_t kSmallFrontier = 16384;
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_scan_small(const uint32_t *q, TravCtl *ctl, const OffT *off,
+                                                       OffT clip, OffT *sc, OffT *rs) {
+    uint64_t F = ctl->F;
+    unsigned long long run = 0;
+    for (uint64_t base = 0; base < F; base += kBlock) {
+        uint64_t i = base + threadIdx.x;
+        OffT d = 0, st = 0;
+        if (i < F) d = clipped_degree(off, q[i], clip, st);
+        unsigned long long tot;
+        unsigned long long ex = block_exclusive_scan((unsigned long long)d, tot);
+        if (i < F) {
+            sc[i] = (OffT)(run + ex);
+            rs[i] = st;
+        }
+        run += tot;
+    }
+    if (threadIdx.x == 0) {
+        sc[F] = (OffT)run;
+        ctl->E = run;
+        ctl->edges_done += run;
+    }
+}
+
 // First frontier row of every 2048-edge expand tile (one thread per tile, so
 // the searches run in parallel instead of inside the expanding CTAs).
 template <class OffT>
@@ -205,6 +232,14 @@ __global__ void k_tile_rows(const OffT *sc, const TravCtl *ctl, uint32_t *tr) {
 
 // Load-balanced top-down expansion of the frontier's (resident) edges.
 // mode: 0 BFS (+1), 1 SSSP (+w), 2 CC (propagate value).
+// Each CTA takes a 2048-edge tile of the flattened frontier edge space.  The
+// row of every edge slot is found without searching: each row writes its
+// index at the slot where its edges start (atomicMax, so zero-degree rows
+// lose to the row that really starts there) and a block-wide max-scan fills
+// the gaps.  Each thread then loads all its edge targets (and weights)
+// before it probes any target, so a thread keeps several independent memory
+// chains in flight.
+constexpr int kExpandBatch = 4;
 template <class OffT, int MODE>
 __global__ void __launch_bounds__(kBlock) k_expand(const uint32_t *q, const OffT *sc, const OffT *rs,
                                                    const uint32_t *tr, const uint32_t *col,
@@ -212,46 +247,105 @@ __global__ void __launch_bounds__(kBlock) k_expand(const uint32_t *q, const OffT
     __shared__ OffT s_sc[kTile + 2];
     __shared__ OffT s_rs[kTile + 2];
     __shared__ uint32_t s_val[kTile + 2];
+    __shared__ uint32_t s_row[kTile];
+    __shared__ uint32_t s_wmax[kBlock / 32];
     const TravCtl *ctl = t.ctl;
     uint64_t E = ctl->E;
     uint32_t thr = ctl->threshold;
     uint64_t ntiles = (E + kTile - 1) / kTile;
+    const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         uint64_t t0 = tile * kTile, t1 = min(E, t0 + kTile);
+        uint32_t len = (uint32_t)(t1 - t0);
         // rows r0..r1 cover the tile (r1 may start exactly at t1: one spare row)
-        uint64_t r0 = tr[tile], nrows = (uint64_t)tr[tile + 1] - r0 + 1;
-        bool staged = nrows <= (uint64_t)kTile + 1;
-        if (staged) {
-            for (uint64_t k = threadIdx.x; k < nrows; k += kBlock) {
+        uint64_t r0 = tr[tile];
+        uint32_t nrows = (uint32_t)((uint64_t)tr[tile + 1] - r0 + 1);
+        if (nrows <= (uint32_t)kTile + 1) {
+            for (uint32_t k = threadIdx.x; k < kTile; k += kBlock) s_row[k] = 0;
+            for (uint32_t k = threadIdx.x; k < nrows; k += kBlock) {
                 s_sc[k] = sc[r0 + k];
                 s_rs[k] = rs[r0 + k];
                 s_val[k] = t.value[q[r0 + k]];
             }
-            if (threadIdx.x == 0) s_sc[nrows] = sc[r0 + nrows];
-        }
-        __syncthreads();
-        for (uint64_t j = t0 + threadIdx.x; j < t1; j += kBlock) {
-            uint64_t row;
-            OffT rsv, scv;
-            uint32_t uval;
-            if (staged) {
-                row = last_le(s_sc, 0, nrows, j);
-                rsv = s_rs[row];
-                scv = s_sc[row];
-                uval = s_val[row];
-            } else {
-                row = last_le(sc, r0, r0 + nrows, j);
-                rsv = rs[row];
-                scv = sc[row];
-                uval = t.value[q[row]];
+            __syncthreads();
+            for (uint32_t k = threadIdx.x; k < nrows; k += kBlock) {
+                uint64_t start = (uint64_t)s_sc[k];
+                uint32_t pos = start > t0 ? (uint32_t)(start - t0) : 0u;
+                if (pos < len) atomicMax(&s_row[pos], k);
             }
-            uint64_t e = (uint64_t)rsv + (j - (uint64_t)scv);
-            uint32_t v = __ldcs(col + e);
-            if (MODE == 0 && t.vis) {
-                relax_bfs(t, v, uval + 1u);
-            } else {
-                uint32_t nd = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + __ldcs(w + e) : uval);
-                relax(t, v, nd, thr);
+            __syncthreads();
+            // inclusive max-scan of s_row: 8 consecutive slots per thread
+            uint32_t loc[kTile / kBlock];
+            uint32_t run = 0;
+#pragma unroll
+            for (int i = 0; i < kTile / kBlock; i++) {
+                run = max(run, s_row[threadIdx.x * (kTile / kBlock) + i]);
+                loc[i] = run;
+            }
+            uint32_t pre = run;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, pre, o);
+                if (lane >= (unsigned)o) pre = max(pre, y);
+            }
+            if (lane == 31) s_wmax[wid] = pre;
+            __syncthreads();
+            uint32_t carry = 0;
+            for (unsigned w2 = 0; w2 < wid; w2++) carry = max(carry, s_wmax[w2]);
+            uint32_t excl = __shfl_up_sync(0xffffffffu, pre, 1);
+            if (lane == 0) excl = 0;
+            carry = max(carry, excl);
+#pragma unroll
+            for (int i = 0; i < kTile / kBlock; i++)
+                s_row[threadIdx.x * (kTile / kBlock) + i] = max(loc[i], carry);
+            __syncthreads();
+            // edges, kExpandBatch per round: all loads first, then the probes
+            for (uint32_t base = threadIdx.x; base < len; base += kBlock * kExpandBatch) {
+                uint32_t v[kExpandBatch], nd[kExpandBatch];
+                bool ok[kExpandBatch];
+#pragma unroll
+                for (int b = 0; b < kExpandBatch; b++) {
+                    uint32_t slot = base + b * kBlock;
+                    ok[b] = slot < len;
+                    v[b] = 0;
+                    nd[b] = 0;
+                    if (ok[b]) {
+                        uint32_t row = s_row[slot];
+                        uint64_t e = (uint64_t)s_rs[row] + (t0 + slot - (uint64_t)s_sc[row]);
+                        v[b] = __ldcs(col + e);
+                        uint32_t uval = s_val[row];
+                        nd[b] = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + __ldcs(w + e) : uval);
+                    }
+                }
+                if (MODE == 0 && t.vis) {
+                    uint32_t word[kExpandBatch];
+#pragma unroll
+                    for (int b = 0; b < kExpandBatch; b++) word[b] = ok[b] ? t.vis[v[b] >> 5] : 0xffffffffu;
+#pragma unroll
+                    for (int b = 0; b < kExpandBatch; b++)
+                        if (!((word[b] >> (v[b] & 31u)) & 1u)) relax_bfs(t, v[b], nd[b]);
+                } else {
+                    uint32_t cur[kExpandBatch];
+#pragma unroll
+                    for (int b = 0; b < kExpandBatch; b++) cur[b] = ok[b] ? t.value[v[b]] : 0u;
+#pragma unroll
+                    for (int b = 0; b < kExpandBatch; b++)
+                        if (nd[b] < cur[b]) relax(t, v[b], nd[b], thr);
+                }
+            }
+        } else {
+            // more rows than slots (zero-degree rows): search each edge's row
+            for (uint64_t j = t0 + threadIdx.x; j < t1; j += kBlock) {
+                uint64_t row = last_le(sc, r0, r0 + nrows, j);
+                uint64_t e = (uint64_t)rs[row] + (j - (uint64_t)sc[row]);
+                uint32_t uval = t.value[q[row]];
+                uint32_t v = __ldcs(col + e);
+                if (MODE == 0 && t.vis) {
+                    relax_bfs(t, v, uval + 1u);
+                } else {
+                    uint32_t nd = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + __ldcs(w + e) : uval);
+                    relax(t, v, nd, thr);
+                }
             }
         }
         __syncthreads();
@@ -292,8 +386,12 @@ __global__ void __launch_bounds__(kBlock) k_bottom_up(uint64_t n, const OffT *of
     const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
     const uint64_t words = (n + 31) / 32;
     const uint64_t chunks = (words + 31) / 32;
-    const uint64_t nwarps_total = (uint64_t)gridDim.x * kBuWarps;
-    for (uint64_t c = (uint64_t)blockIdx.x * kBuWarps + wid; c < chunks; c += nwarps_total) {
+    while (true) {
+        // warps take chunks from a shared counter: chunk costs vary a lot
+        uint64_t c = 0;
+        if (lane == 0) c = atomicAdd(&t.ctl->bu_next, 1u);
+        c = __shfl_sync(0xffffffffu, c, 0);
+        if (c >= chunks) break;
         uint64_t wd = c * 32 + lane;
         uint32_t visw = 0, cand = 0;
         if (wd < words) {
@@ -597,9 +695,14 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         OffT *sc = ws.scan.as<OffT>(), *rs = ws.rowstart.as<OffT>();
 
         // direction decision needs the frontier's edge count first
-        launch(ctx, "k_scan_reduce", k_scan_reduce<OffT>, scan_blocks, kBlock, 0, st, q_cur, d_ctl, off,
-               clip, bsum);
-        launch(ctx, "k_scan_bsums", k_scan_bsums, 1, kBlock, 0, st, bsum, scan_blocks, d_ctl);
+        bool small = F <= kSmallFrontier;
+        if (small) {
+            launch(ctx, "k_scan_small", k_scan_small<OffT>, 1, kBlock, 0, st, q_cur, d_ctl, off, clip, sc, rs);
+        } else {
+            launch(ctx, "k_scan_reduce", k_scan_reduce<OffT>, scan_blocks, kBlock, 0, st, q_cur, d_ctl, off,
+                   clip, bsum);
+            launch(ctx, "k_scan_bsums", k_scan_bsums, 1, kBlock, 0, st, bsum, scan_blocks, d_ctl);
+        }
         uint64_t E = 0;
         if (allow_bu) {
             PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
@@ -617,8 +720,9 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
             launch(ctx, "k_bottom_up", k_bottom_up<OffT>, grid_for((words + 31) / 32, kBuWarps, sms * 6),
                    kBlock, 0, st, n, off, col, bm_cur, (const uint32_t *)g->d_nzbm.as<uint32_t>(), pt);
         } else {
-            launch(ctx, "k_scan_write", k_scan_write<OffT>, scan_blocks, kBlock, 0, st, q_cur, d_ctl, off,
-                   clip, bsum, sc, rs);
+            if (!small)
+                launch(ctx, "k_scan_write", k_scan_write<OffT>, scan_blocks, kBlock, 0, st, q_cur, d_ctl, off,
+                       clip, bsum, sc, rs);
             int eg = sms * 8;
             if (allow_bu) eg = grid_for(E, kTile, sms * 8);
             uint32_t *tr = ws.tiles.as<uint32_t>();
@@ -691,6 +795,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         TravCtl upd = *h_ctl;
         upd.F = (uint32_t)F;
         upd.next_tail = 0;
+        upd.bu_next = 0;
         level_val++;
         upd.level_val = level_val;
         PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &upd, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
