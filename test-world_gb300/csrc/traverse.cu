@@ -145,49 +145,75 @@ __global__ void __launch_bounds__(kBlock) k_scan_write(const uint32_t *q, const 
     if (blockIdx.x == 0 && threadIdx.x == 0) sc[F] = (OffT)ctl->E;
 }
 
+// Where a relaxation pushes.  The next frontier is a bitmap; its queue is
+// built afterwards by k_compact, so no relaxation waits for an atomic's
+// result: the updates below compile to fire-and-forget reductions.
 struct PushTargets {
     uint32_t *value;
-    uint32_t *q_next;
     uint32_t *bm_next;
-    uint32_t *far_q;   // nullptr: no far pile
-    uint32_t *far_bm;
-    TravCtl *ctl;
-    uint32_t cap;      // queue capacity (n)
+    uint32_t *far_bm;  // near/far SSSP: vertices parked above the threshold (nullptr: none)
     uint32_t *vis;     // BFS: visited bitmap (nullptr otherwise)
+    TravCtl *ctl;
 };
 
-// BFS relax: every target of a level gets the same value, so the first claim
-// of the visited bit decides (a 2 MB bitmap stays in L2, the level array does
-// not); the level is a plain store.
+// BFS relax: every target of a level gets the same value, so an unvisited
+// target is marked with a plain store of the level (racing stores write the
+// same value) and a bit in the next frontier; the visited bitmap (2 MB at
+// scale 24, resident in L2) absorbs it when the frontier is compacted.
 __device__ __forceinline__ void relax_bfs(const PushTargets &t, uint32_t v, uint32_t nd) {
     uint32_t bit = 1u << (v & 31u);
     if (t.vis[v >> 5] & bit) return;
-    uint32_t prev = atomicOr(&t.vis[v >> 5], bit);
-    if (prev & bit) return;
     t.value[v] = nd;
     atomicOr(&t.bm_next[v >> 5], bit);
-    warp_append(t.q_next, &t.ctl->next_tail, t.cap, &t.ctl->error, v);
 }
 
-// Relax one edge: the reference's rule (gpu_kernels.cu:126-131), plus the
-// near/far routing and bitmap dedup of the next frontier.
+// Relax one edge whose candidate nd beat the probed value of v: the
+// reference's rule (gpu_kernels.cu:126-131) as a reduction, then v joins the
+// near frontier, or the far pile if nd is at or above the threshold.  When
+// another thread improved v further in between, v is still active, so the
+// extra mark is harmless.
 __device__ __forceinline__ void relax(const PushTargets &t, uint32_t v, uint32_t nd,
                                       uint32_t threshold) {
-    if (nd < t.value[v]) {
-        uint32_t old = atomicMin(&t.value[v], nd);
-        if (nd < old) {
-            uint32_t bit = 1u << (v & 31u);
-            if (nd < threshold || t.far_q == nullptr) {
-                uint32_t prev = atomicOr(&t.bm_next[v >> 5], bit);
-                if (!(prev & bit)) {
-                    warp_append(t.q_next, &t.ctl->next_tail, t.cap, &t.ctl->error, v);
-                    if (t.far_bm && (t.far_bm[v >> 5] & bit)) atomicAnd(&t.far_bm[v >> 5], ~bit);
-                }
-            } else {
-                uint32_t prev = atomicOr(&t.far_bm[v >> 5], bit);
-                if (!(prev & bit))
-                    warp_append(t.far_q, &t.ctl->far_count, t.cap, &t.ctl->error, v);
-            }
+    atomicMin(&t.value[v], nd);
+    uint32_t bit = 1u << (v & 31u);
+    if (nd < threshold || t.far_bm == nullptr) atomicOr(&t.bm_next[v >> 5], bit);
+    else atomicOr(&t.far_bm[v >> 5], bit);
+}
+
+__device__ __forceinline__ void relax_probe(const PushTargets &t, uint32_t v, uint32_t nd,
+                                            uint32_t threshold) {
+    if (nd < t.value[v]) relax(t, v, nd, threshold);
+}
+
+// Build the frontier queue from its bitmap (a warp per 32 words, one atomic
+// per warp for its place in the queue), fold the frontier into the visited
+// bitmap (BFS) and take near vertices out of the far pile (SSSP).
+__global__ void __launch_bounds__(kBlock) k_compact(const uint32_t *bm, uint64_t words, uint32_t *q,
+                                                    TravCtl *ctl, uint32_t *vis, uint32_t *far_bm) {
+    const unsigned lane = lane_id();
+    uint64_t nwarps = (uint64_t)gridDim.x * (kBlock / 32);
+    for (uint64_t c = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); c * 32 < words; c += nwarps) {
+        uint64_t wd = c * 32 + lane;
+        uint32_t word = wd < words ? bm[wd] : 0u;
+        if (word) {
+            if (vis) vis[wd] |= word;
+            if (far_bm) far_bm[wd] &= ~word;
+        }
+        uint32_t cnt = __popc(word), pre = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, pre, o);
+            if (lane >= (unsigned)o) pre += y;
+        }
+        uint32_t total = __shfl_sync(0xffffffffu, pre, 31);
+        uint32_t base = 0;
+        if (lane == 31 && total) base = atomicAdd(&ctl->next_tail, total);
+        base = __shfl_sync(0xffffffffu, base, 31);
+        uint32_t pos = base + pre - cnt;
+        while (word) {
+            int b = __ffs(word) - 1;
+            word &= word - 1;
+            q[pos++] = (uint32_t)(wd * 32 + b);
         }
     }
 }
@@ -344,7 +370,7 @@ __global__ void __launch_bounds__(kBlock) k_expand(const uint32_t *q, const OffT
                     relax_bfs(t, v, uval + 1u);
                 } else {
                     uint32_t nd = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + __ldcs(w + e) : uval);
-                    relax(t, v, nd, thr);
+                    relax_probe(t, v, nd, thr);
                 }
             }
         }
@@ -429,7 +455,6 @@ __global__ void __launch_bounds__(kBlock) k_bottom_up(uint64_t n, const OffT *of
             if (found) {
                 atomicOr(&s_found[wid][(v >> 5) - (uint32_t)(c * 32)], 1u << (v & 31u));
                 t.value[v] = newval;
-                warp_append(t.q_next, &t.ctl->next_tail, t.cap, &t.ctl->error, v);
             }
         }
         __syncwarp();
@@ -505,46 +530,49 @@ __global__ void __launch_bounds__(kBlock) k_relax_partition(uint64_t e_begin, ui
             uint64_t le = j - e_begin;
             uint32_t v = __ldcs(stage_col + le);
             uint32_t nd = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + __ldcs(stage_w + le) : uval);
-            relax(t, v, nd, thr);
+            relax_probe(t, v, nd, thr);
         }
         __syncthreads();
     }
 }
 
-// Near/far: smallest live distance in the far pile.
-__global__ void __launch_bounds__(kBlock) k_far_min(const uint32_t *far_q, const uint32_t *far_bm,
+// Near/far: smallest distance in the far pile (a bitmap).
+__global__ void __launch_bounds__(kBlock) k_far_min(const uint32_t *far_bm, uint64_t words,
                                                     const uint32_t *value, TravCtl *ctl) {
-    uint32_t cnt = ctl->far_count;
     uint32_t best = PTG_UNREACHED;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t v = far_q[i];
-        if (bit_test(far_bm, v)) best = min(best, value[v]);
+    for (uint64_t wd = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; wd < words;
+         wd += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t word = far_bm[wd];
+        while (word) {
+            int b = __ffs(word) - 1;
+            word &= word - 1;
+            best = min(best, value[wd * 32 + b]);
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) best = min(best, __shfl_down_sync(0xffffffffu, best, o));
     if (lane_id() == 0 && best != PTG_UNREACHED) atomicMin(&ctl->far_min, (unsigned long long)best);
 }
 
-// Near/far: move far entries below the new threshold into the (empty) near
-// frontier, keep the rest, drop entries that already moved to near.
-__global__ void __launch_bounds__(kBlock) k_far_split(const uint32_t *far_in, uint32_t *far_out,
-                                                      uint32_t *far_bm, const uint32_t *value,
-                                                      uint32_t *q, uint32_t *bm, TravCtl *ctl,
-                                                      uint32_t cap) {
-    uint32_t cnt = ctl->far_count;
+// Near/far: move the far vertices below the new threshold into the (empty)
+// near frontier bitmap; k_compact then builds its queue.
+__global__ void __launch_bounds__(kBlock) k_far_split(uint32_t *far_bm, uint64_t words,
+                                                      const uint32_t *value, uint32_t *bm,
+                                                      const TravCtl *ctl) {
     uint32_t thr = ctl->threshold;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < cnt;
-         i += (uint64_t)gridDim.x * blockDim.x) {
-        uint32_t v = far_in[i];
-        uint32_t bit = 1u << (v & 31u);
-        if (!(far_bm[v >> 5] & bit)) continue;
-        if (value[v] < thr) {
-            atomicAnd(&far_bm[v >> 5], ~bit);
-            uint32_t prev = atomicOr(&bm[v >> 5], bit);
-            if (!(prev & bit)) warp_append(q, &ctl->next_tail, cap, &ctl->error, v);
-        } else {
-            warp_append(far_out, &ctl->far_tail, cap, &ctl->error, v);
+    for (uint64_t wd = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; wd < words;
+         wd += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t word = far_bm[wd];
+        if (!word) continue;
+        uint32_t moved = 0, rest = word;
+        while (rest) {
+            int b = __ffs(rest) - 1;
+            rest &= rest - 1;
+            if (value[wd * 32 + b] < thr) moved |= 1u << b;
+        }
+        if (moved) {
+            far_bm[wd] = word & ~moved;
+            bm[wd] |= moved;
         }
     }
 }
@@ -574,11 +602,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
     ws.ctl.ensure(sizeof(TravCtl));
     ws.h_ctl.ensure(sizeof(TravCtl));
     bool use_far = kind == TRAV_SSSP && !(flags & PTG_REFERENCE_SCHEDULE);
-    if (use_far) {
-        ws.farq[0].ensure(n * 4);
-        ws.farq[1].ensure(n * 4);
-        ws.farbm.ensure(words * 4);
-    }
+    if (use_far) ws.farbm.ensure(words * 4);
     TravCtl *d_ctl = ws.ctl.as<TravCtl>();
     TravCtl *h_ctl = ws.h_ctl.as<TravCtl>();
     const OffT *off = g->d_off.as<OffT>();
@@ -631,8 +655,10 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         launch(ctx, "k_nonzero_bits", k_nonzero_bits<OffT>, grid_for(words, kBlock, sms * 8), kBlock, 0, st, off,
                n, g->d_nzbm.as<uint32_t>());
     }
-    int cur = 0, far_cur = 0;
-    uint64_t F = init.F, far_count = 0, m_unvisited = g->m;
+    int cur = 0;
+    uint64_t F = init.F, m_unvisited = g->m;
+    bool far_nonempty = false;
+    const int compact_grid = grid_for((words + 31) / 32, kBlock / 32, sms * 8);
     uint32_t threshold = init.threshold, level_val = base;
     bool bottom_up = false;
     if (max_iters == 0) max_iters = (uint32_t)std::min<uint64_t>(0xFFFFFFF0ull, 4 * n + 16);
@@ -648,38 +674,33 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
 
     while (true) {
         if (F == 0) {
-            if (!use_far || far_count == 0) break;
+            if (!use_far || !far_nonempty) break;
             // advance the threshold past the smallest far distance
             unsigned long long big = ~0ull;
             PTG_CUDA_TRY(cudaMemcpyAsync(&d_ctl->far_min, &big, 8, cudaMemcpyHostToDevice, st));
-            launch(ctx, "k_far_min", k_far_min, grid_for(far_count, kBlock, sms * 4), kBlock, 0, st,
-                   ws.farq[far_cur].as<uint32_t>(), ws.farbm.as<uint32_t>(), d_value, d_ctl);
+            launch(ctx, "k_far_min", k_far_min, grid_for(words, kBlock, sms * 8), kBlock, 0, st,
+                   (const uint32_t *)ws.farbm.as<uint32_t>(), words, (const uint32_t *)d_value, d_ctl);
             PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
             PTG_CUDA_TRY(cudaStreamSynchronize(st));
-            if (h_ctl->far_min == ~0ull) break;  // only stale entries left
+            if (h_ctl->far_min == ~0ull) break;  // far pile empty
             uint64_t thr64 = h_ctl->far_min + delta;
             threshold = thr64 >= PTG_UNREACHED ? PTG_UNREACHED : (uint32_t)thr64;
             TravCtl upd = *h_ctl;
             upd.threshold = threshold;
             upd.next_tail = 0;
-            upd.far_tail = 0;
             PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &upd, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
             // bm[cur] is clear (it was the previous round's empty next bitmap)
-            launch(ctx, "k_far_split", k_far_split, grid_for(far_count, kBlock, sms * 8), kBlock, 0, st,
-                ws.farq[far_cur].as<uint32_t>(), ws.farq[far_cur ^ 1].as<uint32_t>(),
-                ws.farbm.as<uint32_t>(), d_value, ws.q[cur].as<uint32_t>(), ws.bm[cur].as<uint32_t>(),
-                d_ctl, (uint32_t)n);
+            launch(ctx, "k_far_split", k_far_split, grid_for(words, kBlock, sms * 8), kBlock, 0, st,
+                   ws.farbm.as<uint32_t>(), words, (const uint32_t *)d_value, ws.bm[cur].as<uint32_t>(),
+                   (const TravCtl *)d_ctl);
+            launch(ctx, "k_compact", k_compact, compact_grid, kBlock, 0, st, (const uint32_t *)ws.bm[cur].as<uint32_t>(),
+                   words, ws.q[cur].as<uint32_t>(), d_ctl, (uint32_t *)nullptr, (uint32_t *)nullptr);
             PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
             PTG_CUDA_TRY(cudaStreamSynchronize(st));
-            PTG_REQUIRE(h_ctl->error == 0, PTG_ERR_CUDA, "frontier overflow in far split");
             F = h_ctl->next_tail;
-            far_count = h_ctl->far_tail;
-            far_cur ^= 1;
             upd = *h_ctl;
             upd.F = (uint32_t)F;
-            upd.far_count = (uint32_t)far_count;
             upd.next_tail = 0;
-            upd.far_tail = 0;
             PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &upd, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
             continue;
         }
@@ -688,8 +709,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         uint32_t *q_cur = ws.q[cur].as<uint32_t>(), *q_nxt = ws.q[cur ^ 1].as<uint32_t>();
         uint32_t *bm_cur = ws.bm[cur].as<uint32_t>(), *bm_nxt = ws.bm[cur ^ 1].as<uint32_t>();
         PTG_CUDA_TRY(cudaMemsetAsync(bm_nxt, 0, words * 4, st));
-        PushTargets pt{d_value, q_nxt, bm_nxt, use_far ? ws.farq[far_cur].as<uint32_t>() : nullptr,
-                       use_far ? ws.farbm.as<uint32_t>() : nullptr, d_ctl, (uint32_t)n, vis};
+        PushTargets pt{d_value, bm_nxt, use_far ? ws.farbm.as<uint32_t>() : nullptr, vis, d_ctl};
         int scan_blocks = grid_for(F, kBlock, kScanBlocks);
         unsigned long long *bsum = ws.bsum.as<unsigned long long>();
         OffT *sc = ws.scan.as<OffT>(), *rs = ws.rowstart.as<OffT>();
@@ -786,12 +806,14 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
                 }
             }
         }
-        // next frontier
+        // next frontier: queue from the bitmap
+        launch(ctx, "k_compact", k_compact, compact_grid, kBlock, 0, st, (const uint32_t *)bm_nxt, words, q_nxt,
+               d_ctl, vis, use_far ? ws.farbm.as<uint32_t>() : (uint32_t *)nullptr);
         PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
         PTG_CUDA_TRY(cudaStreamSynchronize(st));
         PTG_REQUIRE(h_ctl->error == 0, PTG_ERR_CUDA, "frontier overflow in relax");
         F = h_ctl->next_tail;
-        if (use_far) far_count = h_ctl->far_count;
+        if (use_far) far_nonempty = true;
         TravCtl upd = *h_ctl;
         upd.F = (uint32_t)F;
         upd.next_tail = 0;
