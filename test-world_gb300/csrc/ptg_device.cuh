@@ -122,6 +122,22 @@ __device__ __forceinline__ uint64_t block_last_le(const T *a, uint64_t lo, uint6
     return lo;
 }
 
+// L2 policy that evicts first: for edge arrays read once per pass, so they do
+// not push the randomly probed per-vertex arrays out of L2.
+__device__ __forceinline__ uint64_t l2_evict_first_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+// Load through L1 (neighbouring threads reuse the sector) with the L2
+// evict-first hint.
+__device__ __forceinline__ uint32_t ld_edge(const uint32_t *p, uint64_t pol) {
+    uint32_t r;
+    asm volatile("ld.global.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(r) : "l"(p), "l"(pol));
+    return r;
+}
+
 __device__ __forceinline__ bool bit_test(const uint32_t *bm, uint32_t v) {
     return (bm[v >> 5] >> (v & 31u)) & 1u;
 }

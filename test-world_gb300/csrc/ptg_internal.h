@@ -232,6 +232,7 @@ struct ptg_graph {
     ptg::DevBuf d_off, d_col, d_w, d_invdeg;
     ptg::DevBuf d_tiles;  // merge-path tile table (PageRank, CC), built on first use
     ptg::DevBuf d_nzbm;   // bitmap of vertices with edges (bottom-up BFS), built on first use
+    double mean_weight = 0;  // mean resident edge weight (SSSP bucket width), measured on first use
     // out-of-core
     bool out_of_core = false;
     uint64_t resident_edges = 0;

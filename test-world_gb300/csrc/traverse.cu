@@ -258,14 +258,14 @@ __global__ void k_tile_rows(const OffT *sc, const TravCtl *ctl, uint32_t *tr) {
 
 // Load-balanced top-down expansion of the frontier's (resident) edges.
 // mode: 0 BFS (+1), 1 SSSP (+w), 2 CC (propagate value).
-// Each CTA takes a 2048-edge tile of the flattened frontier edge space.  The
-// row of every edge slot is found without searching: each row writes its
-// index at the slot where its edges start (atomicMax, so zero-degree rows
-// lose to the row that really starts there) and a block-wide max-scan fills
-// the gaps.  Each thread then loads all its edge targets (and weights)
-// before it probes any target, so a thread keeps several independent memory
-// chains in flight.
-constexpr int kExpandBatch = 4;
+// Each CTA takes a 2048-edge tile of the flattened frontier edge space and
+// each thread 8 consecutive edge slots of it: one binary search (in shared
+// memory) finds the row of its first slot, later slots advance the row with
+// a register compare.  A thread loads all 8 targets (and weights) before it
+// probes any of them, keeping 8 independent memory chains in flight; edge
+// loads go through L1 (the 32 threads of a warp cover 1 KB of consecutive
+// edges) with an L2 evict-first hint.
+constexpr int kExpandPerThread = kTile / kBlock;
 template <class OffT, int MODE>
 __global__ void __launch_bounds__(kBlock) k_expand(const uint32_t *q, const OffT *sc, const OffT *rs,
                                                    const uint32_t *tr, const uint32_t *col,
@@ -273,13 +273,11 @@ __global__ void __launch_bounds__(kBlock) k_expand(const uint32_t *q, const OffT
     __shared__ OffT s_sc[kTile + 2];
     __shared__ OffT s_rs[kTile + 2];
     __shared__ uint32_t s_val[kTile + 2];
-    __shared__ uint32_t s_row[kTile];
-    __shared__ uint32_t s_wmax[kBlock / 32];
     const TravCtl *ctl = t.ctl;
     uint64_t E = ctl->E;
     uint32_t thr = ctl->threshold;
     uint64_t ntiles = (E + kTile - 1) / kTile;
-    const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+    const uint64_t pol = l2_evict_first_policy();
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         uint64_t t0 = tile * kTile, t1 = min(E, t0 + kTile);
         uint32_t len = (uint32_t)(t1 - t0);
@@ -287,75 +285,54 @@ __global__ void __launch_bounds__(kBlock) k_expand(const uint32_t *q, const OffT
         uint64_t r0 = tr[tile];
         uint32_t nrows = (uint32_t)((uint64_t)tr[tile + 1] - r0 + 1);
         if (nrows <= (uint32_t)kTile + 1) {
-            for (uint32_t k = threadIdx.x; k < kTile; k += kBlock) s_row[k] = 0;
-            for (uint32_t k = threadIdx.x; k < nrows; k += kBlock) {
+            for (uint32_t k = threadIdx.x; k <= nrows; k += kBlock) {
                 s_sc[k] = sc[r0 + k];
-                s_rs[k] = rs[r0 + k];
-                s_val[k] = t.value[q[r0 + k]];
+                if (k < nrows) {
+                    s_rs[k] = rs[r0 + k];
+                    s_val[k] = t.value[q[r0 + k]];
+                }
             }
             __syncthreads();
-            for (uint32_t k = threadIdx.x; k < nrows; k += kBlock) {
-                uint64_t start = (uint64_t)s_sc[k];
-                uint32_t pos = start > t0 ? (uint32_t)(start - t0) : 0u;
-                if (pos < len) atomicMax(&s_row[pos], k);
-            }
-            __syncthreads();
-            // inclusive max-scan of s_row: 8 consecutive slots per thread
-            uint32_t loc[kTile / kBlock];
-            uint32_t run = 0;
+            uint32_t s0 = threadIdx.x * kExpandPerThread;
+            if (s0 < len) {
+                uint64_t j0 = t0 + s0;
+                uint32_t row = (uint32_t)last_le(s_sc, 0, nrows, j0);
+                uint64_t next = (uint64_t)s_sc[row + 1];
+                OffT delta = s_rs[row] - s_sc[row];  // edge index = delta + slot (mod 2^bits)
+                uint32_t uval = s_val[row];
+                uint32_t v[kExpandPerThread], nd[kExpandPerThread];
 #pragma unroll
-            for (int i = 0; i < kTile / kBlock; i++) {
-                run = max(run, s_row[threadIdx.x * (kTile / kBlock) + i]);
-                loc[i] = run;
-            }
-            uint32_t pre = run;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                uint32_t y = __shfl_up_sync(0xffffffffu, pre, o);
-                if (lane >= (unsigned)o) pre = max(pre, y);
-            }
-            if (lane == 31) s_wmax[wid] = pre;
-            __syncthreads();
-            uint32_t carry = 0;
-            for (unsigned w2 = 0; w2 < wid; w2++) carry = max(carry, s_wmax[w2]);
-            uint32_t excl = __shfl_up_sync(0xffffffffu, pre, 1);
-            if (lane == 0) excl = 0;
-            carry = max(carry, excl);
-#pragma unroll
-            for (int i = 0; i < kTile / kBlock; i++)
-                s_row[threadIdx.x * (kTile / kBlock) + i] = max(loc[i], carry);
-            __syncthreads();
-            // edges, kExpandBatch per round: all loads first, then the probes
-            for (uint32_t base = threadIdx.x; base < len; base += kBlock * kExpandBatch) {
-                uint32_t v[kExpandBatch], nd[kExpandBatch];
-                bool ok[kExpandBatch];
-#pragma unroll
-                for (int b = 0; b < kExpandBatch; b++) {
-                    uint32_t slot = base + b * kBlock;
-                    ok[b] = slot < len;
-                    v[b] = 0;
-                    nd[b] = 0;
-                    if (ok[b]) {
-                        uint32_t row = s_row[slot];
-                        uint64_t e = (uint64_t)s_rs[row] + (t0 + slot - (uint64_t)s_sc[row]);
-                        v[b] = __ldcs(col + e);
-                        uint32_t uval = s_val[row];
-                        nd[b] = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + __ldcs(w + e) : uval);
+                for (int b = 0; b < kExpandPerThread; b++) {
+                    uint64_t j = j0 + b;
+                    v[b] = PTG_UNREACHED;
+                    nd[b] = PTG_UNREACHED;
+                    if (s0 + b < len) {
+                        while (j >= next) {  // next row (skips zero-degree rows)
+                            row++;
+                            next = (uint64_t)s_sc[row + 1];
+                            delta = s_rs[row] - s_sc[row];
+                            uval = s_val[row];
+                        }
+                        uint64_t e = (uint64_t)(OffT)(delta + (OffT)j);
+                        v[b] = ld_edge(col + e, pol);
+                        nd[b] = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + ld_edge(w + e, pol) : uval);
                     }
                 }
                 if (MODE == 0 && t.vis) {
-                    uint32_t word[kExpandBatch];
+                    uint32_t word[kExpandPerThread];
 #pragma unroll
-                    for (int b = 0; b < kExpandBatch; b++) word[b] = ok[b] ? t.vis[v[b] >> 5] : 0xffffffffu;
+                    for (int b = 0; b < kExpandPerThread; b++)
+                        word[b] = v[b] != PTG_UNREACHED ? t.vis[v[b] >> 5] : 0xffffffffu;
 #pragma unroll
-                    for (int b = 0; b < kExpandBatch; b++)
+                    for (int b = 0; b < kExpandPerThread; b++)
                         if (!((word[b] >> (v[b] & 31u)) & 1u)) relax_bfs(t, v[b], nd[b]);
                 } else {
-                    uint32_t cur[kExpandBatch];
+                    uint32_t cur[kExpandPerThread];
 #pragma unroll
-                    for (int b = 0; b < kExpandBatch; b++) cur[b] = ok[b] ? t.value[v[b]] : 0u;
+                    for (int b = 0; b < kExpandPerThread; b++)
+                        cur[b] = v[b] != PTG_UNREACHED ? t.value[v[b]] : 0u;
 #pragma unroll
-                    for (int b = 0; b < kExpandBatch; b++)
+                    for (int b = 0; b < kExpandPerThread; b++)
                         if (nd[b] < cur[b]) relax(t, v[b], nd[b], thr);
                 }
             }
@@ -376,6 +353,15 @@ __global__ void __launch_bounds__(kBlock) k_expand(const uint32_t *q, const OffT
         }
         __syncthreads();
     }
+}
+
+// Sum of the resident edge weights (for the default near/far bucket width).
+__global__ void __launch_bounds__(kBlock) k_weight_sum(const uint32_t *w, uint64_t m, unsigned long long *out) {
+    unsigned long long s = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x)
+        s += w[i];
+    s = block_reduce_sum(s);
+    if (threadIdx.x == 0 && s) atomicAdd(out, s);
 }
 
 // Bitmap of vertices with at least one edge (bottom-up BFS never looks at the
@@ -629,7 +615,21 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         init.F = 1;
         init.level_val = base;
         if (use_far) {
-            if (delta == 0) delta = 64;
+            if (delta == 0) {
+                // default bucket width: half the mean edge weight (measured once per graph)
+                if (g->mean_weight == 0 && g->resident_edges > 0) {
+                    ws.bsum.ensure(kScanBlocks * 8);
+                    unsigned long long *acc = ws.bsum.as<unsigned long long>();
+                    PTG_CUDA_TRY(cudaMemsetAsync(acc, 0, 8, st));
+                    launch(ctx, "k_weight_sum", k_weight_sum, grid_for(g->resident_edges, kBlock, sms * 8), kBlock, 0,
+                           st, wt, g->resident_edges, acc);
+                    unsigned long long sum = 0;
+                    PTG_CUDA_TRY(cudaMemcpyAsync(&sum, acc, 8, cudaMemcpyDeviceToHost, st));
+                    PTG_CUDA_TRY(cudaStreamSynchronize(st));
+                    g->mean_weight = std::max(1.0, (double)sum / (double)g->resident_edges);
+                }
+                delta = (uint32_t)std::max(1.0, g->mean_weight > 0 ? g->mean_weight / 2 : 32.0);
+            }
             init.threshold = base + delta;
             PTG_CUDA_TRY(cudaMemsetAsync(ws.farbm.p, 0, words * 4, st));
         }
