@@ -191,8 +191,8 @@ __global__ void __launch_bounds__(kBlock) k_spmv(PrArgs a) {
         uint32_t first_row = NONE;
         ff first_val{0.f, 0.f};
         ff sum{0.f, 0.f};
+        uint32_t end_l = li < nrows ? (uint32_t)(s_end[li] - (OffT)j0) : 0xFFFFFFFFu;
         for (uint32_t k = td0; k < td1; k++) {
-            uint32_t end_l = li < nrows ? (uint32_t)(s_end[li] - (OffT)j0) : 0xFFFFFFFFu;
             if (lj >= end_l) {
                 if (cont) {  // combined with earlier threads after the scan
                     first_row = li;
@@ -204,6 +204,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv(PrArgs a) {
                 row_start = end_l;
                 sum = ff{0.f, 0.f};
                 li++;
+                end_l = li < nrows ? (uint32_t)(s_end[li] - (OffT)j0) : 0xFFFFFFFFu;
             } else {
                 sum = ff_add(sum, s_val[lj]);
                 lj++;
