@@ -1,10 +1,11 @@
 // batch.cu - multi-source BFS / SSSP entry points.
 //
 // ptg_msbfs / ptg_mssssp take k sources and fill k rows of results, each row
-// equal to a single-source ptg_bfs / ptg_sssp call.  The fused kernels
-// (64 sources per bitmask word) live in msbfs.cu; this file holds the entry
-// points and the row-by-row schedule used for graphs the fused path does not
-// cover.
+// equal to a single-source ptg_bfs / ptg_sssp call.  Sources are processed in
+// groups of 64 (one 64-bit mask word per vertex, msbfs.cu); host outputs are
+// produced group by group in a device buffer of 64 rows and copied out while
+// the next group runs.  Graphs the fused kernels do not cover (out-of-core)
+// run the single-source traversal row by row.
 #include <algorithm>
 #include <cstring>
 
@@ -13,8 +14,8 @@
 using namespace ptg;
 
 namespace ptg {
-bool msbfs_fused(ptg_graph *g, const uint32_t *sources, uint32_t k, uint32_t *d_out, bool weighted,
-                 uint32_t flags, RunResult &rr);
+bool ms_group(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_rows, bool weighted,
+              uint32_t flags, RunResult &rr);
 }
 
 extern "C" {
@@ -35,25 +36,24 @@ static ptg_status ms_common(ptg_graph *g, const uint32_t *sources, uint32_t k, u
         PTG_CUDA_TRY(cudaEventRecord(ctx->ev0, st));
         bool out_dev = flags & PTG_OUT_DEVICE;
         uint64_t n = g->n;
-        // rows are produced in device memory; host outputs are copied per row
-        DevBuf rowbuf;
-        uint32_t *d_all = nullptr;
-        if (out_dev) d_all = out;
-        bool fused = msbfs_fused(g, sources, k, d_all, weighted, flags, rr);
-        if (!fused) {
-            if (!out_dev) rowbuf.ensure(n * 4);
-            for (uint32_t i = 0; i < k; i++) {
-                uint32_t *d_row = out_dev ? out + (uint64_t)i * n : rowbuf.as<uint32_t>();
-                RunResult r1;
-                run_traversal(g, weighted ? TRAV_SSSP : TRAV_BFS, sources[i], d_row, flags,
-                              opts ? opts->delta : 0, opts ? opts->max_iterations : 0, r1);
-                rr.iterations += r1.iterations;
-                rr.edges_relaxed += r1.edges_relaxed;
-                rr.link_bytes += r1.link_bytes;
-                if (!out_dev)
-                    PTG_CUDA_TRY(cudaMemcpyAsync(out + (uint64_t)i * n, d_row, n * 4,
-                                                 cudaMemcpyDeviceToHost, st));
+        DevBuf rows;
+        if (!out_dev) rows.ensure(64 * n * 4);
+        for (uint32_t g0 = 0; g0 < k; g0 += 64) {
+            uint32_t cnt = std::min<uint32_t>(64, k - g0);
+            uint32_t *d_rows = out_dev ? out + (uint64_t)g0 * n : rows.as<uint32_t>();
+            if (!ms_group(g, sources + g0, cnt, d_rows, weighted, flags, rr)) {
+                for (uint32_t i = 0; i < cnt; i++) {
+                    RunResult r1;
+                    run_traversal(g, weighted ? TRAV_SSSP : TRAV_BFS, sources[g0 + i], d_rows + (uint64_t)i * n,
+                                  flags, opts ? opts->delta : 0, opts ? opts->max_iterations : 0, r1);
+                    rr.iterations += r1.iterations;
+                    rr.edges_relaxed += r1.edges_relaxed;
+                    rr.link_bytes += r1.link_bytes;
+                }
             }
+            if (!out_dev)
+                PTG_CUDA_TRY(cudaMemcpyAsync(out + (uint64_t)g0 * n, d_rows, (uint64_t)cnt * n * 4,
+                                             cudaMemcpyDeviceToHost, st));
         }
         PTG_CUDA_TRY(cudaEventRecord(ctx->ev1, st));
         PTG_CUDA_TRY(cudaStreamSynchronize(st));

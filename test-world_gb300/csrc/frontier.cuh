@@ -1,0 +1,125 @@
+// frontier.cuh - degree scan of a frontier queue and the tiling of its
+// flattened edge space (shared by the traversal and multi-source kernels).
+//
+// Given a queue q[0..F) of vertices, these kernels compute sc[i] = exclusive
+// prefix sum of the (clipped) degrees, rs[i] = adjacency start of q[i],
+// sc[F] = E and ctl->E = E; k_tile_rows then gives, for every 2048-edge tile
+// of [0, E), the queue index of the row holding its first edge.  The
+// reference does this with Thrust scans over all n labels every round
+// (ptGraph/main.cu:1307-1317).
+#pragma once
+
+#include "ptg_device.cuh"
+
+namespace ptg {
+namespace {
+
+// Degree of frontier entry i, clipped to the resident edge prefix.
+template <class OffT>
+__device__ __forceinline__ OffT clipped_degree(const OffT *off, uint32_t u, OffT clip, OffT &start) {
+    OffT b = off[u], e = off[u + 1];
+    start = b;
+    if (e > clip) e = clip;
+    return e > b ? (OffT)(e - b) : (OffT)0;
+}
+
+// Pass 1 of the frontier degree scan: per-CTA sums over contiguous slices.
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_scan_reduce(const uint32_t *q, const TravCtl *ctl,
+                                                        const OffT *off, OffT clip,
+                                                        unsigned long long *bsum) {
+    uint64_t F = ctl->F;
+    uint64_t per = (F + gridDim.x - 1) / gridDim.x;
+    uint64_t lo = min(F, (uint64_t)blockIdx.x * per), hi = min(F, lo + per);
+    unsigned long long s = 0;
+    for (uint64_t i = lo + threadIdx.x; i < hi; i += kBlock) {
+        OffT st;
+        s += clipped_degree(off, q[i], clip, st);
+    }
+    s = block_reduce_sum(s);
+    if (threadIdx.x == 0) bsum[blockIdx.x] = s;
+}
+
+// Pass 2: one CTA turns the per-CTA sums into exclusive offsets; ctl->E = total.
+__global__ void __launch_bounds__(kBlock) k_scan_bsums(unsigned long long *bsum, int nb,
+                                                       TravCtl *ctl) {
+    unsigned long long carry = 0;
+    for (int base = 0; base < nb; base += kBlock) {
+        int i = base + threadIdx.x;
+        unsigned long long x = i < nb ? bsum[i] : 0ull, tot;
+        unsigned long long ex = block_exclusive_scan(x, tot);
+        if (i < nb) bsum[i] = carry + ex;
+        carry += tot;
+    }
+    if (threadIdx.x == 0) {
+        ctl->E = carry;
+        ctl->edges_done += carry;
+    }
+}
+
+// Pass 3: per-CTA scan of its slice; writes sc[i] (exclusive prefix of the
+// clipped degrees), rs[i] (adjacency start of q[i]) and sc[F] = E.
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_scan_write(const uint32_t *q, const TravCtl *ctl,
+                                                       const OffT *off, OffT clip,
+                                                       const unsigned long long *bsum, OffT *sc,
+                                                       OffT *rs) {
+    uint64_t F = ctl->F;
+    uint64_t per = (F + gridDim.x - 1) / gridDim.x;
+    uint64_t lo = min(F, (uint64_t)blockIdx.x * per), hi = min(F, lo + per);
+    unsigned long long run = bsum[blockIdx.x];
+    for (uint64_t base = lo; base < hi; base += kBlock) {
+        uint64_t i = base + threadIdx.x;
+        OffT d = 0, st = 0;
+        if (i < hi) d = clipped_degree(off, q[i], clip, st);
+        unsigned long long tot;
+        unsigned long long ex = block_exclusive_scan((unsigned long long)d, tot);
+        if (i < hi) {
+            sc[i] = (OffT)(run + ex);
+            rs[i] = st;
+        }
+        run += tot;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc[F] = (OffT)ctl->E;
+}
+
+// Small frontiers (most rounds): one CTA does the work of k_scan_reduce,
+// k_scan_bsums and k_scan_write in a single launch.
+constexpr uint32_t kSmallFrontier = 16384;
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_scan_small(const uint32_t *q, TravCtl *ctl, const OffT *off,
+                                                       OffT clip, OffT *sc, OffT *rs) {
+    uint64_t F = ctl->F;
+    unsigned long long run = 0;
+    for (uint64_t base = 0; base < F; base += kBlock) {
+        uint64_t i = base + threadIdx.x;
+        OffT d = 0, st = 0;
+        if (i < F) d = clipped_degree(off, q[i], clip, st);
+        unsigned long long tot;
+        unsigned long long ex = block_exclusive_scan((unsigned long long)d, tot);
+        if (i < F) {
+            sc[i] = (OffT)(run + ex);
+            rs[i] = st;
+        }
+        run += tot;
+    }
+    if (threadIdx.x == 0) {
+        sc[F] = (OffT)run;
+        ctl->E = run;
+        ctl->edges_done += run;
+    }
+}
+
+// First frontier row of every 2048-edge expand tile (one thread per tile, so
+// the searches run in parallel instead of inside the expanding CTAs).
+template <class OffT>
+__global__ void k_tile_rows(const OffT *sc, const TravCtl *ctl, uint32_t *tr) {
+    uint64_t F = ctl->F, E = ctl->E;
+    uint64_t ntiles = (E + kTile - 1) / kTile;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t <= ntiles;
+         t += (uint64_t)gridDim.x * blockDim.x)
+        tr[t] = (uint32_t)last_le(sc, 0, F, min(t * (uint64_t)kTile, E));
+}
+
+}  // namespace
+}  // namespace ptg

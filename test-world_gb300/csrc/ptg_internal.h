@@ -203,7 +203,8 @@ struct Prof {
 // context / graph
 // --------------------------------------------------------------------------
 struct Workspace {
-    DevBuf value, q[2], bm[2], farq[2], farbm, vis, scan, rowstart, tiles, bsum, ctl, aux, aux2, flags;
+    DevBuf value, q[2], bm[2], farbm, vis, scan, rowstart, tiles, bsum, ctl, aux, aux2, flags;
+    DevBuf ms[3];  // multi-source 64-bit masks
     PinnedBuf h_ctl, h_flags;
 };
 

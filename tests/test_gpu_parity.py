@@ -210,6 +210,25 @@ def test_msbfs_equals_single_source(ptg, ctx):
         assert (ss[i] == G.sssp(int(s))).all()
 
 
+@pytest.mark.parametrize("symmetric", [True, False])
+def test_multi_source_groups_vs_oracle(ptg, ctx, oracle, symmetric):
+    """Several 64-source groups (130 sources), both push and pull levels."""
+    off, col, w = ptg.gen_rmat(14, 16, seed=6, symmetric=symmetric, wmin=1, wmax=63)
+    G = ctx.graph(off, col, w, symmetric=symmetric)
+    rng = np.random.default_rng(14)
+    srcs = rng.integers(0, off.size - 1, 130).astype(np.uint32)
+    ms = G.msbfs(srcs)
+    for i in range(0, 130, 13):
+        assert (ms[i] == oracle.bfs(off, col, int(srcs[i]), method="queue")).all()
+    for i in range(130):
+        assert (ms[i] == G.bfs(int(srcs[i]))).all()
+    ss = G.mssssp(srcs[:70])
+    for i in range(0, 70, 7):
+        assert (ss[i] == oracle.sssp(off, col, w, int(srcs[i]))).all()
+    for i in range(70):
+        assert (ss[i] == G.sssp(int(srcs[i]))).all()
+
+
 def test_cc_batch_matches_per_graph(ptg, ctx, oracle):
     vb, off, col = ptg.gen_er_batch(64, 50, 5000, 8.0, seed=11)
     lab = ctx.cc_batch(vb, off, col)
