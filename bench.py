@@ -46,10 +46,102 @@ def parse():
     p.add_argument("--sssp-sources", type=int, default=4)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--workload", default="suite", choices=["suite", "batch"],
+                   help="suite: the in-HBM suite on RMAT-24 (default); batch: 1024-source MS-BFS/MS-SSSP "
+                        "on RMAT-22 and CC over a batch of ER graphs, each against one-at-a-time calls")
+    p.add_argument("--er-graphs", type=int, default=4096)
+    p.add_argument("--batch-sources", type=int, default=1024)
     p.add_argument("--profile-case", action="store_true",
                    help="run one SSSP, one 20-iteration PageRank and one BFS (in that order) on the "
                         "workload graph and exit: the small fixed case ncu captures run on")
     return p.parse_args()
+
+
+def batch_workload(args):
+    """Config 4: batched queries against the plain one-at-a-time path (same results checked)."""
+    import torch
+    import ptgraph
+    ctx = ptgraph.Ctx(int(os.environ.get("LOCAL_RANK", "0")))
+    scale = 22 if args.scale == 24 else args.scale
+    off, col, w = ptgraph.gen_rmat(scale, 16, 0.57, 0.19, 0.19, seed=4, symmetric=True, wmin=1, wmax=63)
+    n, m = off.size - 1, col.size
+    deg = np.diff(off.astype(np.int64))
+    rng = np.random.default_rng(4)
+    k = args.batch_sources
+    srcs = rng.choice(np.nonzero(deg)[0], k, replace=False).astype(np.uint32)
+    G = ctx.graph(off.astype(np.uint32), col, w, symmetric=True)
+    out = torch.empty((k, n), dtype=torch.int32, device="cuda")
+    one = torch.empty(n, dtype=torch.int32, device="cuda")
+    res = {"graph": {"scale": scale, "n": n, "m": m}, "sources": k}
+    sample = min(64, k)
+    for name, multi, single in (("bfs", G.msbfs, G.bfs), ("sssp", G.mssssp, G.sssp)):
+        st = {}
+        multi_dev(G, srcs, out, name, st)  # warm-up
+        t = []
+        for _ in range(2):
+            st = {}
+            multi_dev(G, srcs, out, name, st)
+            t.append(st["device_ms"])
+        batched_ms = min(t)
+        plain_ms = 0.0
+        for s in srcs[:sample]:
+            st = {}
+            single(int(s), flags=ptgraph.PTG_OUT_DEVICE, stats=st, out=one)
+            plain_ms += st["device_ms"]
+            if name == "bfs":
+                pass
+        plain_ms *= k / sample
+        # identical results on a sample of rows
+        for i in range(0, k, max(1, k // 8)):
+            single(int(srcs[i]), flags=ptgraph.PTG_OUT_DEVICE, out=one)
+            assert torch.equal(out[i], one), name
+        res[name] = {"batched_ms": batched_ms, "plain_ms_extrapolated": plain_ms,
+                     "batched_queries_per_s": k / batched_ms * 1e3, "plain_queries_per_s": k / plain_ms * 1e3,
+                     "speedup": plain_ms / batched_ms, "plain_sample": sample}
+    # CC over a batch of ER graphs
+    t0 = time.time()
+    vb, eoff, ecol = ptgraph.gen_er_batch(args.er_graphs, 1000, 1000000, 8.0, seed=7)
+    gen_s = time.time() - t0
+    st = {}
+    labels = ctx.cc_batch(vb, eoff, ecol, stats=st)
+    st = {}
+    labels = ctx.cc_batch(vb, eoff, ecol, stats=st)
+    batch_ms = st["device_ms"]
+    psample = min(128, args.er_graphs)
+    plain_ms = 0.0
+    for gi in range(psample):
+        a, b = int(vb[gi]), int(vb[gi + 1])
+        e0, e1 = int(eoff[a]), int(eoff[b])
+        loff = (eoff[a:b + 1] - eoff[a]).astype(np.uint32)
+        lcol = (ecol[e0:e1] - a).astype(np.uint32)
+        Gi = ctx.graph(loff, lcol, symmetric=True)
+        sti = {}
+        li = Gi.cc(stats=sti)
+        plain_ms += sti["device_ms"]
+        assert (li == labels[a:b]).all()
+        Gi.close()
+    plain_ms *= args.er_graphs / psample
+    res["cc_batch"] = {"graphs": args.er_graphs, "vertices": int(vb[-1]), "edges": int(ecol.size),
+                       "batched_ms": batch_ms, "plain_ms_extrapolated": plain_ms,
+                       "batched_graphs_per_s": args.er_graphs / batch_ms * 1e3,
+                       "plain_graphs_per_s": args.er_graphs / plain_ms * 1e3, "speedup": plain_ms / batch_ms,
+                       "plain_sample": psample, "gen_s": gen_s,
+                       "note": "device time of the kernels; plain = one ptg_cc launch sequence per graph"}
+    print(json.dumps({"workload": "batched", "metric": "batched_queries_per_s", "results": res}))
+
+
+def multi_dev(G, srcs, out, name, st):
+    import ctypes
+    import ptgraph
+    o = ptgraph.RunOpts()
+    o.flags = ptgraph.PTG_OUT_DEVICE
+    rs = ptgraph.RunStats()
+    o.stats = ctypes.pointer(rs)
+    s = np.ascontiguousarray(srcs, dtype=np.uint32)
+    fn = ptgraph.lib().ptg_msbfs if name == "bfs" else ptgraph.lib().ptg_mssssp
+    ptgraph._check(fn(G.h, s.ctypes.data_as(ptgraph._u32p), s.size, ctypes.c_void_p(out.data_ptr()),
+                      ctypes.byref(o)), G.ctx.h)
+    st.update(rs.as_dict())
 
 
 def profile_case(args):
@@ -218,6 +310,9 @@ def main():
         return
     if args.profile_case:
         profile_case(args)
+        return
+    if args.workload == "batch":
+        batch_workload(args)
         return
     import torch
     import ptgraph
