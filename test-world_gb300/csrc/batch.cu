@@ -16,6 +16,7 @@ using namespace ptg;
 namespace ptg {
 bool ms_group(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_rows, bool weighted,
               uint32_t flags, RunResult &rr);
+uint32_t ms_group_size(bool weighted);
 }
 
 extern "C" {
@@ -36,10 +37,11 @@ static ptg_status ms_common(ptg_graph *g, const uint32_t *sources, uint32_t k, u
         PTG_CUDA_TRY(cudaEventRecord(ctx->ev0, st));
         bool out_dev = flags & PTG_OUT_DEVICE;
         uint64_t n = g->n;
+        const uint32_t group = ms_group_size(weighted);
         DevBuf rows;
-        if (!out_dev) rows.ensure(64 * n * 4);
-        for (uint32_t g0 = 0; g0 < k; g0 += 64) {
-            uint32_t cnt = std::min<uint32_t>(64, k - g0);
+        if (!out_dev) rows.ensure((uint64_t)std::min(group, k) * n * 4);
+        for (uint32_t g0 = 0; g0 < k; g0 += group) {
+            uint32_t cnt = std::min<uint32_t>(group, k - g0);
             uint32_t *d_rows = out_dev ? out + (uint64_t)g0 * n : rows.as<uint32_t>();
             if (!ms_group(g, sources + g0, cnt, d_rows, weighted, flags, rr)) {
                 for (uint32_t i = 0; i < cnt; i++) {

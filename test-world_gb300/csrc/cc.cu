@@ -88,33 +88,6 @@ __global__ void __launch_bounds__(kBlock) k_hook(uint64_t e_begin, uint64_t e_en
     }
 }
 
-// Hook every edge of a resident graph, tile by tile along the graph's
-// merge-path tiling (rows [i0, i1], edges [j0, j1) per tile, precomputed), so
-// no CTA searches for its rows.
-template <class OffT>
-__global__ void __launch_bounds__(kBlock) k_hook_tiles(const OffT *off, const uint32_t *col,
-                                                       const uint64_t *tiles, uint64_t n, uint64_t m,
-                                                       int tile_items, uint32_t *parent) {
-    extern __shared__ unsigned char smem_raw[];
-    OffT *s_start = reinterpret_cast<OffT *>(smem_raw);
-    uint64_t total = n + m;
-    uint64_t ntiles = (total + tile_items - 1) / tile_items;
-    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        uint64_t d0 = tile * (uint64_t)tile_items, d1 = min(total, d0 + tile_items);
-        uint64_t i0 = tiles[tile], i1 = tiles[tile + 1];
-        uint64_t j0 = d0 - i0, j1 = d1 - i1;
-        uint64_t nrows = i1 - i0;
-        for (uint64_t k = threadIdx.x; k <= nrows; k += kBlock) s_start[k] = off[i0 + k];
-        __syncthreads();
-        for (uint64_t j = j0 + threadIdx.x; j < j1; j += kBlock) {
-            uint64_t u = i0 + last_le(s_start, 0, nrows + 1, j);
-            uint32_t v = __ldcs(col + j);
-            if (v < u) hook(parent, (uint32_t)u, v);
-        }
-        __syncthreads();
-    }
-}
-
 // Point every vertex at its root; labels become local ids (minus base).
 __global__ void k_compress(uint32_t *parent, uint64_t n, uint64_t first, uint32_t base) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
@@ -144,15 +117,7 @@ void cc_hook_impl(ptg_graph *g, uint32_t *d_label, RunResult &rr) {
     const OffT *off = g->d_off.as<OffT>();
     launch(ctx, "k_iota", k_iota, grid_for(n, kBlock, sms * 8), kBlock, 0, st, d_label, n, (uint64_t)0);
     uint64_t res = g->resident_edges;
-    if (!g->out_of_core && res > 0) {
-        int items = merge_tile_items();
-        const uint64_t *tiles = merge_tiles(g);
-        uint64_t ntiles = (n + g->m + items - 1) / items;
-        launch(ctx, "k_hook_tiles", k_hook_tiles<OffT>, grid_for(ntiles, 1, sms * 8), kBlock,
-               (size_t)(items + 1) * sizeof(OffT), st, off, g->d_col.as<uint32_t>(), tiles, n, g->m, items,
-               d_label);
-        PTG_CUDA_TRY(cudaGetLastError());
-    } else if (res > 0) {
+    if (res > 0) {
         uint64_t v_last = g->out_of_core ? g->part_first_vertex[g->resident_partitions] : n - 1;
         if (v_last >= n) v_last = n - 1;
         launch(ctx, "k_hook", k_hook<OffT>, grid_for(res, kTile, sms * 16), kBlock, 0, st, (uint64_t)0, res,
@@ -187,18 +152,57 @@ void cc_hook_impl(ptg_graph *g, uint32_t *d_label, RunResult &rr) {
 }
 
 // ---------------------------------------------------------------------------
-// batch: many independent graphs in one concatenated CSR.  Graphs are
-// disjoint vertex ranges, so one union-find over global ids handles all of
-// them in a single edge pass; labels are localized at the end.
+// Afforest (Sutton, Ben-Nun, Barak 2018) on symmetric graphs: link every
+// vertex to its first neighbours, compress, find each graph's largest
+// component from a few samples, then link the remaining edges only of
+// vertices outside it.  An edge between the giant component and a vertex w
+// outside it is still linked from w's side, so the result is unchanged; on
+// RMAT and ER graphs almost every vertex is in the giant component and most
+// of the edge list is never read.
 // ---------------------------------------------------------------------------
-// Persistent edge pass: CTAs pull 2048-edge tiles of the concatenated edge
-// array from a global counter until none are left (one launch for the whole
-// batch, however uneven the graphs are).
-__global__ void __launch_bounds__(kBlock) k_hook_persistent(const unsigned long long *off,
-                                                            const uint32_t *col, uint64_t n,
-                                                            uint64_t m, uint32_t *parent,
-                                                            unsigned long long *tile_counter) {
-    __shared__ unsigned long long s_off[kTile + 2];
+constexpr uint32_t kAffRounds = 2;
+
+template <class OffT>
+__global__ void k_aff_sample(const OffT *off, const uint32_t *col, uint64_t n, uint32_t r, uint32_t *parent) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
+        OffT b = off[v], e = off[v + 1];
+        if (e - b > (OffT)r) hook(parent, (uint32_t)v, col[b + r]);
+    }
+}
+
+// Largest component of each graph: the majority label of 9 spread samples.
+__global__ void k_aff_giant(const uint64_t *vb, uint32_t num_graphs, const uint32_t *parent, uint32_t *giant) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < num_graphs; g += gridDim.x * blockDim.x) {
+        uint64_t v0 = vb[g], nv = vb[g + 1] - v0;
+        uint32_t lab[9];
+        for (int i = 0; i < 9; i++) {
+            uint64_t h = (uint64_t)(g + 1) * 0x9E3779B97F4A7C15ull + (uint64_t)i * 0xBF58476D1CE4E5B9ull;
+            h ^= h >> 31;
+            lab[i] = nv ? parent[v0 + h % nv] : 0u;
+        }
+        uint32_t best = lab[0];
+        int bestc = 0;
+        for (int i = 0; i < 9; i++) {
+            int c = 0;
+            for (int j = 0; j < 9; j++) c += lab[j] == lab[i];
+            if (c > bestc) {
+                bestc = c;
+                best = lab[i];
+            }
+        }
+        giant[g] = best;
+    }
+}
+
+// Link the edges from the kAffRounds-th neighbour on of every vertex outside
+// its graph's giant component.  CTAs pull 2048-edge tiles from a counter.
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_aff_finish(const OffT *off, const uint32_t *col, uint64_t n, uint64_t m,
+                                                       const uint64_t *vb, uint32_t num_graphs,
+                                                       const uint32_t *giant, uint32_t *parent,
+                                                       unsigned long long *tile_counter) {
+    __shared__ OffT s_off[kTile + 2];
+    __shared__ uint8_t s_skip[kTile + 1];
     __shared__ uint64_t s_tile;
     uint64_t ntiles = (m + kTile - 1) / kTile;
     while (true) {
@@ -212,21 +216,83 @@ __global__ void __launch_bounds__(kBlock) k_hook_persistent(const unsigned long 
         uint64_t r1 = block_last_le(off, r0, n, t1 - 1);
         uint64_t nrows = r1 - r0 + 1;
         bool staged = nrows <= (uint64_t)kTile;
-        if (staged)
-            for (uint64_t k = threadIdx.x; k <= nrows; k += kBlock) s_off[k] = off[r0 + k];
+        if (staged) {
+            for (uint64_t k = threadIdx.x; k <= nrows; k += kBlock) {
+                s_off[k] = off[r0 + k];
+                if (k < nrows) {
+                    uint64_t u = r0 + k;
+                    uint32_t gi = num_graphs == 1 ? 0u : (uint32_t)last_le(vb, 0, num_graphs, u);
+                    s_skip[k] = parent[u] == giant[gi];
+                }
+            }
+        }
         __syncthreads();
         for (uint64_t j = t0 + threadIdx.x; j < t1; j += kBlock) {
-            uint64_t u = staged ? r0 + last_le(s_off, 0, nrows, j) : last_le(off, r0, r0 + nrows, j);
-            uint32_t v = col[j];
-            if (v < u) hook(parent, (uint32_t)u, v);
+            uint64_t u, rs;
+            bool skip;
+            if (staged) {
+                uint64_t k = last_le(s_off, 0, nrows, j);
+                u = r0 + k;
+                rs = s_off[k];
+                skip = s_skip[k];
+            } else {
+                u = last_le(off, r0, r0 + nrows, j);
+                rs = off[u];
+                uint32_t gi = num_graphs == 1 ? 0u : (uint32_t)last_le(vb, 0, num_graphs, u);
+                skip = parent[u] == giant[gi];
+            }
+            if (skip || j - rs < kAffRounds) continue;
+            hook(parent, (uint32_t)u, __ldcs(col + j));
         }
         __syncthreads();
     }
 }
 
+// The whole Afforest sequence on a resident CSR of one or more graphs.
+template <class OffT>
+void afforest(ptg_ctx *ctx, const OffT *off, const uint32_t *col, uint64_t n, uint64_t m, const uint64_t *d_vb,
+              uint32_t num_graphs, uint32_t *parent, uint32_t *d_giant, unsigned long long *d_counter) {
+    cudaStream_t st = ctx->stream;
+    const int sms = ctx->sm_count;
+    int vgrid = grid_for(n, kBlock, sms * 8);
+    launch(ctx, "k_iota", k_iota, vgrid, kBlock, 0, st, parent, n, (uint64_t)0);
+    for (uint32_t r = 0; r < kAffRounds; r++) {
+        launch(ctx, "k_aff_sample", k_aff_sample<OffT>, vgrid, kBlock, 0, st, off, col, n, r, parent);
+        launch(ctx, "k_compress", k_compress, vgrid, kBlock, 0, st, parent, n, (uint64_t)0, 0u);
+    }
+    launch(ctx, "k_aff_giant", k_aff_giant, grid_for(num_graphs, kBlock, sms * 4), kBlock, 0, st, d_vb, num_graphs,
+           (const uint32_t *)parent, d_giant);
+    PTG_CUDA_TRY(cudaMemsetAsync(d_counter, 0, 8, st));
+    int occ = 0;
+    PTG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_aff_finish<OffT>, kBlock, 0));
+    launch(ctx, "k_aff_finish", k_aff_finish<OffT>, std::max(1, occ) * sms, kBlock, 0, st, off, col, n, m, d_vb,
+           num_graphs, (const uint32_t *)d_giant, parent, d_counter);
+    launch(ctx, "k_compress", k_compress, vgrid, kBlock, 0, st, parent, n, (uint64_t)0, 0u);
+    PTG_CUDA_TRY(cudaGetLastError());
+}
+
 }  // namespace
 
 void run_cc_hook(ptg_graph *g, uint32_t *d_label, RunResult &rr) {
+    if (!g->out_of_core && g->m > 0) {
+        // resident symmetric graph: Afforest
+        Workspace &ws = g->ctx->ws;
+        ws.bsum.ensure(1024 * 8);
+        uint64_t *d_vb = ws.bsum.as<uint64_t>();
+        uint32_t *d_giant = reinterpret_cast<uint32_t *>(d_vb + 2);
+        unsigned long long *d_counter = reinterpret_cast<unsigned long long *>(d_vb + 4);
+        uint64_t vb[2] = {0, g->n};
+        PTG_CUDA_TRY(cudaMemcpyAsync(d_vb, vb, 16, cudaMemcpyHostToDevice, g->ctx->stream));
+        if (g->off64)
+            afforest<unsigned long long>(g->ctx, g->d_off.as<unsigned long long>(), g->d_col.as<uint32_t>(), g->n,
+                                         g->m, d_vb, 1, d_label, d_giant, d_counter);
+        else
+            afforest<uint32_t>(g->ctx, g->d_off.as<uint32_t>(), g->d_col.as<uint32_t>(), g->n, g->m, d_vb, 1,
+                               d_label, d_giant, d_counter);
+        rr.edges_relaxed = g->m;
+        rr.iterations = 1;
+        return;
+    }
     if (g->off64) cc_hook_impl<unsigned long long>(g, d_label, rr);
     else cc_hook_impl<uint32_t>(g, d_label, rr);
 }
@@ -238,26 +304,22 @@ void run_cc_batch(ptg_ctx *ctx, uint32_t num_graphs, const uint64_t *vtx_begin,
     uint64_t n = vtx_begin[num_graphs];
     uint64_t m = offsets[n];
     PTG_REQUIRE(n < 0xFFFFFFFFull, PTG_ERR_INVALID, "batched CC needs fewer than 2^32 vertices in total");
-    DevBuf d_off, d_col, d_parent, d_vb, d_counter;
+    DevBuf d_off, d_col, d_parent, d_vb, d_counter, d_giant;
     d_off.ensure((n + 1) * 8);
     d_col.ensure(std::max<uint64_t>(m, 1) * 4);
     d_parent.ensure(n * 4);
     d_vb.ensure((num_graphs + 1) * 8);
     d_counter.ensure(8);
+    d_giant.ensure((uint64_t)num_graphs * 4);
     PTG_CUDA_TRY(cudaMemcpyAsync(d_off.p, offsets, (n + 1) * 8, cudaMemcpyHostToDevice, st));
     if (m) PTG_CUDA_TRY(cudaMemcpyAsync(d_col.p, col, m * 4, cudaMemcpyHostToDevice, st));
     PTG_CUDA_TRY(cudaMemcpyAsync(d_vb.p, vtx_begin, (num_graphs + 1) * 8, cudaMemcpyHostToDevice, st));
-    PTG_CUDA_TRY(cudaMemsetAsync(d_counter.p, 0, 8, st));
     PTG_CUDA_TRY(cudaEventRecord(ctx->ev0, st));
-    launch(ctx, "k_iota", k_iota, grid_for(n, kBlock, sms * 8), kBlock, 0, st, d_parent.as<uint32_t>(), n,
-           (uint64_t)0);
-    int occ = 0;
-    PTG_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_hook_persistent, kBlock, 0));
-    launch(ctx, "k_hook_persistent", k_hook_persistent, std::max(1, occ) * sms, kBlock, 0, st,
-           d_off.as<unsigned long long>(), d_col.as<uint32_t>(), n, m, d_parent.as<uint32_t>(),
-           d_counter.as<unsigned long long>());
-    launch(ctx, "k_compress", k_compress, grid_for(n, kBlock, sms * 8), kBlock, 0, st,
-           d_parent.as<uint32_t>(), n, (uint64_t)0, 0u);
+    // one Afforest pass over the concatenated CSR: a single persistent launch
+    // links the remaining edges of every graph, however uneven the graphs are
+    afforest<unsigned long long>(ctx, d_off.as<unsigned long long>(), d_col.as<uint32_t>(), n, m,
+                                 d_vb.as<uint64_t>(), num_graphs, d_parent.as<uint32_t>(), d_giant.as<uint32_t>(),
+                                 d_counter.as<unsigned long long>());
     launch(ctx, "k_localize", k_localize, grid_for(n, kBlock, sms * 8), kBlock, 0, st,
            d_parent.as<uint32_t>(), d_parent.as<uint32_t>(), n, d_vb.as<uint64_t>(), num_graphs);
     PTG_CUDA_TRY(cudaGetLastError());

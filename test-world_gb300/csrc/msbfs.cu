@@ -1,18 +1,19 @@
-// msbfs.cu - fused multi-source BFS and SSSP: 64 sources per 64-bit mask word.
+// msbfs.cu - fused multi-source BFS and SSSP over 64-bit source masks.
 //
 // The reference answers one source per call (bfsCaculateIn*/ssspCaculateIn*,
 // ptGraph/main.cu:24-44); a batch of sources there is a loop of full calls
-// (testBFS, main.cu:537-556).  Here one traversal serves up to 64 sources:
+// (testBFS, main.cu:537-556).  Here one traversal serves many sources:
 //
-// MS-BFS (after Then et al., "The More the Merrier"): per vertex a 64-bit
-//   frontier mask F[v] (which sources reached v in the last level) and a seen
-//   mask S[v].  A level either pushes (active vertices OR their F into their
-//   neighbours' next masks, load-balanced over the frontier's edges like the
-//   single-source expand) or, when the frontier is large and the graph is
-//   symmetric, pulls (every vertex ORs its neighbours' F, stopping as soon as
-//   every source has seen it).  One edge read serves all 64 sources.
+// MS-BFS (after Then et al., "The More the Merrier"): per vertex W 64-bit
+//   words of frontier mask F[v] (which of up to 64*W sources reached v in the
+//   last level) and seen mask S[v].  A level either pushes (active vertices OR
+//   their F into the next masks of their neighbours, load-balanced over the
+//   frontier's edges like the single-source expand) or, when the frontier's
+//   edges are a large share of the graph and the graph is symmetric, pulls
+//   (every vertex ORs its neighbours' F, stopping once all sources saw it).
+//   With W = 4 one 32-byte sector read per edge serves 256 sources.
 // MS-SSSP: distances stored vertex-major, dist[v*64 + s], so the 64 distances
-//   of a vertex are two 128-byte lines; a warp relaxes one edge for all 64
+//   of a vertex are two 128-byte lines; a warp relaxes one edge for 64
 //   sources at once (lane l handles sources l and l+32), only for sources
 //   whose distance at the edge's tail improved in the previous round (a
 //   64-bit active mask per vertex); improvements set bits of the target's
@@ -28,59 +29,65 @@ namespace {
 
 typedef unsigned long long u64;
 
-// Seed: masks of the sources (several sources may share a vertex).
-__global__ void k_ms_seed(const uint32_t *srcs, uint32_t k, u64 *F, u64 *S, uint32_t *out, uint64_t n,
-                          uint32_t base, int vertex_major_dist) {
+// ---------------------------------------------------------------------------
+// MS-BFS, W mask words per vertex (layout M[v*W + w])
+// ---------------------------------------------------------------------------
+template <int W>
+__global__ void k_msb_seed(const uint32_t *srcs, uint32_t k, u64 *F, u64 *S, uint32_t *out, uint64_t n,
+                           uint32_t base) {
     for (uint32_t i = threadIdx.x; i < k; i += blockDim.x) {
         uint32_t s = srcs[i];
-        atomicOr(&F[s], 1ull << i);
-        if (S) atomicOr(&S[s], 1ull << i);
-        if (vertex_major_dist) out[(uint64_t)s * 64 + i] = base;
-        else out[(uint64_t)i * n + s] = base;
+        atomicOr(&F[(uint64_t)s * W + i / 64], 1ull << (i % 64));
+        atomicOr(&S[(uint64_t)s * W + i / 64], 1ull << (i % 64));
+        out[(uint64_t)i * n + s] = base;
     }
 }
 
-// Queue of vertices whose mask is non-zero (warp-aggregated appends), plus
-// the sum of their degrees (ctl->E) for the push/pull choice.
-template <class OffT>
-__global__ void __launch_bounds__(kBlock) k_ms_queue(const u64 *M, uint64_t n, const OffT *off, uint32_t *q,
-                                                     TravCtl *ctl) {
+// Queue of vertices with a non-zero mask, and the sum of their degrees
+// (ctl->m_unvisited) for the push/pull choice.
+template <class OffT, int W>
+__global__ void __launch_bounds__(kBlock) k_msb_queue(const u64 *M, uint64_t n, const OffT *off, uint32_t *q,
+                                                      TravCtl *ctl) {
     unsigned long long degsum = 0;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
-        bool act = M[v] != 0ull;
-        unsigned ballot = __ballot_sync(__activemask(), act);
+        bool act = false;
+#pragma unroll
+        for (int w = 0; w < W; w++) act |= M[v * W + w] != 0ull;
         if (act) {
             degsum += (unsigned long long)(off[v + 1] - off[v]);
             warp_append(q, &ctl->next_tail, (unsigned)n, &ctl->error, (uint32_t)v);
         }
-        (void)ballot;
     }
     degsum = block_reduce_sum(degsum);
     if (threadIdx.x == 0 && degsum) atomicAdd(&ctl->m_unvisited, degsum);
 }
 
-// Write level `val` into out[i*n + v] for every source bit i in nb; the warp
+// Write level `val` into out[s*n + v] for every source bit s in nb; the warp
 // loops over the union of its lanes' bits so each store is coalesced.
-__device__ __forceinline__ void ms_write_levels(uint32_t *out, uint64_t n, uint64_t v, bool valid, u64 nb,
-                                                uint32_t val) {
-    u64 any = nb;
+template <int W>
+__device__ __forceinline__ void msb_write_levels(uint32_t *out, uint64_t n, uint64_t v, bool valid,
+                                                 const u64 (&nb)[W], uint32_t val) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) any |= __shfl_xor_sync(0xffffffffu, any, o);
-    while (any) {
-        int i = __ffsll((long long)any) - 1;
-        any &= any - 1;
-        if (valid && ((nb >> i) & 1ull)) out[(uint64_t)i * n + v] = val;
+    for (int w = 0; w < W; w++) {
+        u64 any = nb[w];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) any |= __shfl_xor_sync(0xffffffffu, any, o);
+        while (any) {
+            int i = __ffsll((long long)any) - 1;
+            any &= any - 1;
+            if (valid && ((nb[w] >> i) & 1ull)) out[(uint64_t)(w * 64 + i) * n + v] = val;
+        }
     }
 }
 
 // Push level: every edge (u -> v) of the frontier ORs F[u] into N[v].
-template <class OffT>
-__global__ void __launch_bounds__(kBlock) k_ms_push(const uint32_t *q, const OffT *sc, const OffT *rs,
-                                                    const uint32_t *tr, const uint32_t *col, const u64 *F,
-                                                    const u64 *S, u64 *N, const TravCtl *ctl) {
+template <class OffT, int W>
+__global__ void __launch_bounds__(kBlock) k_msb_push(const uint32_t *q, const OffT *sc, const OffT *rs,
+                                                     const uint32_t *tr, const uint32_t *col, const u64 *F,
+                                                     const u64 *S, u64 *N, const TravCtl *ctl) {
     __shared__ OffT s_sc[kTile + 2];
     __shared__ OffT s_rs[kTile + 2];
-    __shared__ u64 s_f[kTile + 2];
+    __shared__ uint32_t s_u[kTile + 2];
     uint64_t E = ctl->E;
     uint64_t ntiles = (E + kTile - 1) / kTile;
     for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -93,7 +100,7 @@ __global__ void __launch_bounds__(kBlock) k_ms_push(const uint32_t *q, const Off
                 s_sc[k] = sc[r0 + k];
                 if (k < nrows) {
                     s_rs[k] = rs[r0 + k];
-                    s_f[k] = F[q[r0 + k]];
+                    s_u[k] = q[r0 + k];
                 }
             }
         }
@@ -102,36 +109,45 @@ __global__ void __launch_bounds__(kBlock) k_ms_push(const uint32_t *q, const Off
             uint64_t row = staged ? last_le(s_sc, 0, nrows, j) : last_le(sc, r0, r0 + nrows, j);
             OffT rsv = staged ? s_rs[row] : rs[row];
             OffT scv = staged ? s_sc[row] : sc[row];
-            u64 f = staged ? s_f[row] : F[q[row]];
+            uint32_t u = staged ? s_u[row] : q[row];
             uint32_t v = __ldcs(col + (uint64_t)rsv + (j - (uint64_t)scv));
-            u64 add = f & ~S[v];
-            if (add) atomicOr(&N[v], add);
+#pragma unroll
+            for (int w = 0; w < W; w++) {
+                u64 add = F[(uint64_t)u * W + w] & ~S[(uint64_t)v * W + w];
+                if (add) atomicOr(&N[(uint64_t)v * W + w], add);
+            }
         }
         __syncthreads();
     }
 }
 
 // After a push: N[v] &= ~S[v], S |= N, levels written, next queue built.
-template <class OffT>
-__global__ void __launch_bounds__(kBlock) k_ms_update(uint64_t n, const OffT *off, u64 *N, u64 *S,
-                                                      uint32_t *out, uint32_t val, uint32_t *q, TravCtl *ctl) {
+template <class OffT, int W>
+__global__ void __launch_bounds__(kBlock) k_msb_update(uint64_t n, const OffT *off, u64 *N, u64 *S,
+                                                       uint32_t *out, uint32_t val, uint32_t *q, TravCtl *ctl) {
     unsigned long long degsum = 0;
     uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     uint64_t span = (n + 31) / 32 * 32;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < span; v += stride) {
         bool valid = v < n;
-        u64 nb = 0;
-        if (valid) {
-            u64 x = N[v];
-            if (x) {
-                u64 s = S[v];
-                nb = x & ~s;
-                N[v] = nb;
-                if (nb) S[v] = s | nb;
+        u64 nb[W];
+        bool any = false;
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+            nb[w] = 0;
+            if (valid) {
+                u64 x = N[v * W + w];
+                if (x) {
+                    u64 s = S[v * W + w];
+                    nb[w] = x & ~s;
+                    N[v * W + w] = nb[w];
+                    if (nb[w]) S[v * W + w] = s | nb[w];
+                }
             }
+            any |= nb[w] != 0ull;
         }
-        ms_write_levels(out, n, v, valid, nb, val);
-        if (nb) {
+        msb_write_levels<W>(out, n, v, valid, nb, val);
+        if (any) {
             degsum += (unsigned long long)(off[v + 1] - off[v]);
             warp_append(q, &ctl->next_tail, (unsigned)n, &ctl->error, (uint32_t)v);
         }
@@ -141,37 +157,60 @@ __global__ void __launch_bounds__(kBlock) k_ms_update(uint64_t n, const OffT *of
 }
 
 // Pull level (symmetric graphs): N[v] = (OR of F over v's neighbours) & ~S[v],
-// stopping early once every source has seen v.
-template <class OffT>
-__global__ void __launch_bounds__(kBlock) k_ms_pull(uint64_t n, const OffT *off, const uint32_t *col,
-                                                    const u64 *F, u64 *S, u64 *N, u64 all, uint32_t *out,
-                                                    uint32_t val, uint32_t *q, TravCtl *ctl) {
+// stopping early once every source has seen v.  A neighbour's W words are one
+// 32-byte sector for W = 4.
+template <class OffT, int W>
+__global__ void __launch_bounds__(kBlock) k_msb_pull(uint64_t n, const OffT *off, const uint32_t *col,
+                                                     const u64 *F, u64 *S, u64 *N, const u64 *all_words,
+                                                     uint32_t *out, uint32_t val, uint32_t *q, TravCtl *ctl) {
     unsigned long long degsum = 0;
+    u64 all[W];
+#pragma unroll
+    for (int w = 0; w < W; w++) all[w] = all_words[w];
     uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     uint64_t span = (n + 31) / 32 * 32;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < span; v += stride) {
         bool valid = v < n;
-        u64 nb = 0;
+        u64 nb[W];
+        bool any = false;
+#pragma unroll
+        for (int w = 0; w < W; w++) nb[w] = 0;
         if (valid) {
-            u64 s = S[v];
-            if (s != all) {
+            u64 s[W];
+            bool full = true;
+#pragma unroll
+            for (int w = 0; w < W; w++) {
+                s[w] = S[v * W + w];
+                full &= s[w] == all[w];
+            }
+            if (!full) {
                 OffT b = off[v], e = off[v + 1];
-                u64 acc = 0;
-                for (OffT k = b; k < e; k += 4) {
+                u64 acc[W];
+#pragma unroll
+                for (int w = 0; w < W; w++) acc[w] = 0;
+                for (OffT k = b; k < e; k += 2) {
                     uint32_t c0 = col[k];
                     uint32_t c1 = k + 1 < e ? col[k + 1] : c0;
-                    uint32_t c2 = k + 2 < e ? col[k + 2] : c0;
-                    uint32_t c3 = k + 3 < e ? col[k + 3] : c0;
-                    acc |= F[c0] | F[c1] | F[c2] | F[c3];
-                    if ((acc | s) == all) break;
+                    bool done = true;
+#pragma unroll
+                    for (int w = 0; w < W; w++) {
+                        acc[w] |= F[(uint64_t)c0 * W + w] | F[(uint64_t)c1 * W + w];
+                        done &= (acc[w] | s[w]) == all[w];
+                    }
+                    if (done) break;
                 }
-                nb = acc & ~s;
-                if (nb) S[v] = s | nb;
+#pragma unroll
+                for (int w = 0; w < W; w++) {
+                    nb[w] = acc[w] & ~s[w];
+                    if (nb[w]) S[v * W + w] = s[w] | nb[w];
+                    any |= nb[w] != 0ull;
+                }
             }
-            N[v] = nb;
+#pragma unroll
+            for (int w = 0; w < W; w++) N[v * W + w] = nb[w];
         }
-        ms_write_levels(out, n, v, valid, nb, val);
-        if (nb) {
+        msb_write_levels<W>(out, n, v, valid, nb, val);
+        if (any) {
             degsum += (unsigned long long)(off[v + 1] - off[v]);
             warp_append(q, &ctl->next_tail, (unsigned)n, &ctl->error, (uint32_t)v);
         }
@@ -180,13 +219,24 @@ __global__ void __launch_bounds__(kBlock) k_ms_pull(uint64_t n, const OffT *off,
     if (threadIdx.x == 0 && degsum) atomicAdd(&ctl->m_unvisited, degsum);
 }
 
+// ---------------------------------------------------------------------------
+// MS-SSSP (64 sources per group)
+// ---------------------------------------------------------------------------
+__global__ void k_mss_seed(const uint32_t *srcs, uint32_t k, u64 *A, uint32_t *dist, uint32_t base) {
+    for (uint32_t i = threadIdx.x; i < k; i += blockDim.x) {
+        uint32_t s = srcs[i];
+        atomicOr(&A[s], 1ull << i);
+        dist[(uint64_t)s * 64 + i] = base;
+    }
+}
+
 // MS-SSSP round: a warp relaxes one edge at a time for all 64 sources (lane l:
 // sources l and l+32), four edges per step so eight distance loads per lane
 // are in flight.  Edge slots are tiled like the single-source expand.
 template <class OffT>
-__global__ void __launch_bounds__(kBlock) k_ms_relax(const uint32_t *q, const OffT *sc, const OffT *rs,
-                                                     const uint32_t *tr, const uint32_t *col, const uint32_t *w,
-                                                     uint32_t *dist, const u64 *A, u64 *N, const TravCtl *ctl) {
+__global__ void __launch_bounds__(kBlock) k_mss_relax(const uint32_t *q, const OffT *sc, const OffT *rs,
+                                                      const uint32_t *tr, const uint32_t *col, const uint32_t *w,
+                                                      uint32_t *dist, const u64 *A, u64 *N, const TravCtl *ctl) {
     __shared__ OffT s_sc[kTile + 2];
     __shared__ OffT s_rs[kTile + 2];
     __shared__ uint32_t s_u[kTile + 2];
@@ -228,14 +278,12 @@ __global__ void __launch_bounds__(kBlock) k_ms_relax(const uint32_t *q, const Of
             uint32_t du0 = dist[(uint64_t)u * 64 + lane], du1 = dist[(uint64_t)u * 64 + 32 + lane];
             for (uint64_t j = w0; j < w1; j += 4) {
                 uint32_t vv[4], ww[4], cur0[4], cur1[4], nd0[4], nd1[4];
-                bool ok[4];
 #pragma unroll
                 for (int b = 0; b < 4; b++) {
                     uint64_t jj = j + b;
-                    ok[b] = jj < w1;
                     vv[b] = 0;
                     nd0[b] = nd1[b] = PTG_UNREACHED;
-                    if (ok[b]) {
+                    if (jj < w1) {
                         while (jj >= next) {
                             row++;
                             row_info(row, next, delta, u);
@@ -270,8 +318,8 @@ __global__ void __launch_bounds__(kBlock) k_ms_relax(const uint32_t *q, const Of
 }
 
 // dist[v*64 + s] -> out[s*n + v] for s < k (32 vertices x 64 sources per tile).
-__global__ void __launch_bounds__(kBlock) k_ms_transpose(const uint32_t *dist, uint64_t n, uint32_t k,
-                                                         uint32_t *out) {
+__global__ void __launch_bounds__(kBlock) k_mss_transpose(const uint32_t *dist, uint64_t n, uint32_t k,
+                                                          uint32_t *out) {
     __shared__ uint32_t t[32][65];
     for (uint64_t v0 = (uint64_t)blockIdx.x * 32; v0 < n; v0 += (uint64_t)gridDim.x * 32) {
         for (int i = threadIdx.x; i < 32 * 64; i += kBlock) {
@@ -287,9 +335,75 @@ __global__ void __launch_bounds__(kBlock) k_ms_transpose(const uint32_t *dist, u
     }
 }
 
+// ---------------------------------------------------------------------------
+// host driver
+// ---------------------------------------------------------------------------
+struct MsState {
+    ptg_ctx *ctx;
+    Workspace *ws;
+    cudaStream_t st;
+    TravCtl *d_ctl, *h_ctl;
+    uint32_t *q, *qn;
+};
+
+// Frontier degree scan + tile rows for the queue in ws.q[0] (count in ctl->F).
 template <class OffT>
-void ms_group_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_rows, bool weighted,
-                   uint32_t flags, RunResult &rr) {
+void ms_scan(ptg_ctx *ctx, Workspace &ws, const OffT *off, uint64_t m, uint64_t F, TravCtl *d_ctl) {
+    cudaStream_t st = ctx->stream;
+    const int sms = ctx->sm_count;
+    OffT *sc = ws.scan.as<OffT>(), *rs = ws.rowstart.as<OffT>();
+    unsigned long long *bsum = ws.bsum.as<unsigned long long>();
+    const uint32_t *q = ws.q[0].as<uint32_t>();
+    if (F <= kSmallFrontier) {
+        launch(ctx, "k_scan_small", k_scan_small<OffT>, 1, kBlock, 0, st, q, d_ctl, off, (OffT)m, sc, rs);
+    } else {
+        int nb = grid_for(F, kBlock, 1024);
+        launch(ctx, "k_scan_reduce", k_scan_reduce<OffT>, nb, kBlock, 0, st, q, (const TravCtl *)d_ctl, off, (OffT)m,
+               bsum);
+        launch(ctx, "k_scan_bsums", k_scan_bsums, 1, kBlock, 0, st, bsum, nb, d_ctl);
+        launch(ctx, "k_scan_write", k_scan_write<OffT>, nb, kBlock, 0, st, q, (const TravCtl *)d_ctl, off, (OffT)m,
+               (const unsigned long long *)bsum, sc, rs);
+    }
+    launch(ctx, "k_tile_rows", k_tile_rows<OffT>, sms * 4, kBlock, 0, st, (const OffT *)sc, (const TravCtl *)d_ctl,
+           ws.tiles.as<uint32_t>());
+}
+
+template <class OffT>
+void ms_prepare(ptg_graph *g, uint64_t mask_bytes) {
+    Workspace &ws = g->ctx->ws;
+    uint64_t n = g->n, m = g->m;
+    ws.ms[0].ensure(mask_bytes);
+    ws.ms[1].ensure(mask_bytes);
+    ws.ms[2].ensure(mask_bytes);
+    ws.q[0].ensure(n * 4);
+    ws.q[1].ensure(n * 4);
+    ws.scan.ensure((n + 1) * sizeof(OffT));
+    ws.rowstart.ensure((n + 1) * sizeof(OffT));
+    ws.tiles.ensure((m / kTile + 4) * 4);
+    ws.bsum.ensure(1024 * 8 + 256 * 4 + 64);
+    ws.ctl.ensure(sizeof(TravCtl));
+    ws.h_ctl.ensure(sizeof(TravCtl));
+}
+
+// Read back the control block, take the new queue, reset counters.
+inline void ms_next(ptg_ctx *ctx, Workspace &ws, uint64_t &F, uint64_t &Eact, uint64_t &E) {
+    cudaStream_t st = ctx->stream;
+    TravCtl *d_ctl = ws.ctl.as<TravCtl>(), *h_ctl = ws.h_ctl.as<TravCtl>();
+    PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
+    PTG_CUDA_TRY(cudaStreamSynchronize(st));
+    PTG_REQUIRE(h_ctl->error == 0, PTG_ERR_CUDA, "frontier overflow in multi-source round");
+    F = h_ctl->next_tail;
+    Eact = h_ctl->m_unvisited;
+    E = h_ctl->E;
+    std::swap(ws.q[0].p, ws.q[1].p);
+    std::swap(ws.q[0].bytes, ws.q[1].bytes);
+    TravCtl upd{};
+    upd.F = (uint32_t)F;
+    PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &upd, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
+}
+
+template <class OffT, int W>
+void msbfs_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_rows, uint32_t flags, RunResult &rr) {
     ptg_ctx *ctx = g->ctx;
     Workspace &ws = ctx->ws;
     cudaStream_t st = ctx->stream;
@@ -298,126 +412,138 @@ void ms_group_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d
     const OffT *off = g->d_off.as<OffT>();
     const uint32_t *col = g->d_col.as<uint32_t>();
     uint32_t base = (flags & PTG_LEVEL_ZERO_BASED) ? 0u : 1u;
-
-    ws.ms[0].ensure(n * 8);
-    ws.ms[1].ensure(n * 8);
-    if (!weighted) ws.ms[2].ensure(n * 8);
-    ws.q[0].ensure(n * 4);
-    ws.scan.ensure((n + 1) * sizeof(OffT));
-    ws.rowstart.ensure((n + 1) * sizeof(OffT));
-    ws.tiles.ensure((m / kTile + 4) * 4);
-    ws.bsum.ensure(1024 * 8 + 64 * 4);
-    ws.ctl.ensure(sizeof(TravCtl));
-    ws.h_ctl.ensure(sizeof(TravCtl));
-    u64 *M0 = ws.ms[0].as<u64>(), *M1 = ws.ms[1].as<u64>();
-    u64 *S = weighted ? nullptr : ws.ms[2].as<u64>();
-    uint32_t *q = ws.q[0].as<uint32_t>();
-    OffT *sc = ws.scan.as<OffT>(), *rs = ws.rowstart.as<OffT>();
-    uint32_t *tr = ws.tiles.as<uint32_t>();
+    ms_prepare<OffT>(g, n * 8 * W);
+    u64 *M0 = ws.ms[0].as<u64>(), *M1 = ws.ms[1].as<u64>(), *S = ws.ms[2].as<u64>();
     unsigned long long *bsum = ws.bsum.as<unsigned long long>();
     uint32_t *d_srcs = reinterpret_cast<uint32_t *>(bsum + 1024);
+    u64 *d_all = reinterpret_cast<u64 *>(d_srcs + 256);
     TravCtl *d_ctl = ws.ctl.as<TravCtl>();
-    TravCtl *h_ctl = ws.h_ctl.as<TravCtl>();
-
-    uint32_t *dist = nullptr;
-    if (weighted) {
-        ws.aux.ensure(n * 64 * 4);
-        dist = ws.aux.as<uint32_t>();
-        PTG_CUDA_TRY(cudaMemsetAsync(dist, 0xFF, n * 64 * 4, st));
-    } else {
-        PTG_CUDA_TRY(cudaMemsetAsync(d_rows, 0xFF, (uint64_t)k * n * 4, st));
-        PTG_CUDA_TRY(cudaMemsetAsync(S, 0, n * 8, st));
+    PTG_CUDA_TRY(cudaMemsetAsync(d_rows, 0xFF, (uint64_t)k * n * 4, st));
+    PTG_CUDA_TRY(cudaMemsetAsync(S, 0, n * 8 * W, st));
+    PTG_CUDA_TRY(cudaMemsetAsync(M0, 0, n * 8 * W, st));
+    PTG_CUDA_TRY(cudaMemsetAsync(M1, 0, n * 8 * W, st));
+    u64 all[W];
+    for (int w = 0; w < W; w++) {
+        int bits = std::max(0, std::min(64, (int)k - 64 * w));
+        all[w] = bits == 64 ? ~0ull : ((1ull << bits) - 1ull);
     }
-    PTG_CUDA_TRY(cudaMemsetAsync(M0, 0, n * 8, st));
-    PTG_CUDA_TRY(cudaMemsetAsync(M1, 0, n * 8, st));
     PTG_CUDA_TRY(cudaMemcpyAsync(d_srcs, h_srcs, k * 4, cudaMemcpyHostToDevice, st));
-    launch(ctx, "k_ms_seed", k_ms_seed, 1, 64, 0, st, (const uint32_t *)d_srcs, k, M0, S,
-           weighted ? dist : d_rows, n, base, weighted ? 1 : 0);
+    PTG_CUDA_TRY(cudaMemcpyAsync(d_all, all, sizeof(all), cudaMemcpyHostToDevice, st));
+    launch(ctx, "k_msb_seed", k_msb_seed<W>, 1, 256, 0, st, (const uint32_t *)d_srcs, k, M0, S, d_rows, n, base);
     TravCtl init{};
     PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &init, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
     int vgrid = grid_for(n, kBlock, sms * 8);
-    launch(ctx, "k_ms_queue", k_ms_queue<OffT>, vgrid, kBlock, 0, st, (const u64 *)M0, n, off, q, d_ctl);
-    PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
-    PTG_CUDA_TRY(cudaStreamSynchronize(st));
-    uint64_t F = h_ctl->next_tail, Eact = h_ctl->m_unvisited;
-    u64 all = k == 64 ? ~0ull : ((1ull << k) - 1ull);
+    launch(ctx, "k_msb_queue", k_msb_queue<OffT, W>, vgrid, kBlock, 0, st, (const u64 *)M0, n, off,
+           ws.q[1].as<uint32_t>(), d_ctl);
+    uint64_t F, Eact, E;
+    ms_next(ctx, ws, F, Eact, E);
     uint32_t level = base;
     int cur = 0;
+    const uint32_t max_rounds = (uint32_t)std::min<uint64_t>(0xFFFFFFF0ull, n + 16);
+    while (F > 0) {
+        if (rr.iterations >= max_rounds) throw Error{PTG_ERR_TIMEOUT, "iteration limit reached"};
+        rr.iterations++;
+        u64 *Mc = cur ? M1 : M0, *Mn = cur ? M0 : M1;
+        bool pull = g->symmetric && Eact * 10 > m;
+        if (pull) {
+            launch(ctx, "k_msb_pull", k_msb_pull<OffT, W>, vgrid, kBlock, 0, st, n, off, col, (const u64 *)Mc, S, Mn,
+                   (const u64 *)d_all, d_rows, level + 1, ws.q[1].as<uint32_t>(), d_ctl);
+        } else {
+            ms_scan<OffT>(ctx, ws, off, m, F, d_ctl);
+            PTG_CUDA_TRY(cudaMemsetAsync(Mn, 0, n * 8 * W, st));
+            launch(ctx, "k_msb_push", k_msb_push<OffT, W>, sms * 8, kBlock, 0, st, (const uint32_t *)ws.q[0].p,
+                   (const OffT *)ws.scan.p, (const OffT *)ws.rowstart.p, (const uint32_t *)ws.tiles.p, col,
+                   (const u64 *)Mc, (const u64 *)S, Mn, (const TravCtl *)d_ctl);
+            launch(ctx, "k_msb_update", k_msb_update<OffT, W>, vgrid, kBlock, 0, st, n, off, Mn, S, d_rows,
+                   level + 1, ws.q[1].as<uint32_t>(), d_ctl);
+        }
+        PTG_CUDA_TRY(cudaGetLastError());
+        ms_next(ctx, ws, F, Eact, E);
+        rr.edges_relaxed += pull ? 0 : E;
+        cur ^= 1;
+        level++;
+    }
+}
+
+template <class OffT>
+void mssssp_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_rows, uint32_t flags,
+                 RunResult &rr) {
+    ptg_ctx *ctx = g->ctx;
+    Workspace &ws = ctx->ws;
+    cudaStream_t st = ctx->stream;
+    const uint64_t n = g->n, m = g->m;
+    const int sms = ctx->sm_count;
+    const OffT *off = g->d_off.as<OffT>();
+    const uint32_t *col = g->d_col.as<uint32_t>();
     const uint32_t *wt = g->d_w.as<uint32_t>();
+    uint32_t base = (flags & PTG_LEVEL_ZERO_BASED) ? 0u : 1u;
+    ms_prepare<OffT>(g, n * 8);
+    u64 *M0 = ws.ms[0].as<u64>(), *M1 = ws.ms[1].as<u64>();
+    unsigned long long *bsum = ws.bsum.as<unsigned long long>();
+    uint32_t *d_srcs = reinterpret_cast<uint32_t *>(bsum + 1024);
+    TravCtl *d_ctl = ws.ctl.as<TravCtl>();
+    ws.aux.ensure(n * 64 * 4);
+    uint32_t *dist = ws.aux.as<uint32_t>();
+    PTG_CUDA_TRY(cudaMemsetAsync(dist, 0xFF, n * 64 * 4, st));
+    PTG_CUDA_TRY(cudaMemsetAsync(M0, 0, n * 8, st));
+    PTG_CUDA_TRY(cudaMemsetAsync(M1, 0, n * 8, st));
+    PTG_CUDA_TRY(cudaMemcpyAsync(d_srcs, h_srcs, k * 4, cudaMemcpyHostToDevice, st));
+    launch(ctx, "k_mss_seed", k_mss_seed, 1, 64, 0, st, (const uint32_t *)d_srcs, k, M0, dist, base);
+    TravCtl init{};
+    PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &init, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
+    int vgrid = grid_for(n, kBlock, sms * 8);
+    launch(ctx, "k_msb_queue", k_msb_queue<OffT, 1>, vgrid, kBlock, 0, st, (const u64 *)M0, n, off,
+           ws.q[1].as<uint32_t>(), d_ctl);
+    uint64_t F, Eact, E;
+    ms_next(ctx, ws, F, Eact, E);
+    int cur = 0;
     const uint32_t max_rounds = (uint32_t)std::min<uint64_t>(0xFFFFFFF0ull, 4 * n + 16);
     while (F > 0) {
         if (rr.iterations >= max_rounds) throw Error{PTG_ERR_TIMEOUT, "iteration limit reached"};
         rr.iterations++;
         u64 *Mc = cur ? M1 : M0, *Mn = cur ? M0 : M1;
-        TravCtl upd{};
-        upd.F = (uint32_t)F;
-        PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &upd, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
-        bool pull = !weighted && g->symmetric && Eact * 12 > m;
-        uint32_t *qn = ws.q[1].p ? ws.q[1].as<uint32_t>() : nullptr;
-        ws.q[1].ensure(n * 4);
-        qn = ws.q[1].as<uint32_t>();
-        if (pull) {
-            launch(ctx, "k_ms_pull", k_ms_pull<OffT>, vgrid, kBlock, 0, st, n, off, col, (const u64 *)Mc, S, Mn,
-                   all, d_rows, level + 1, qn, d_ctl);
-        } else {
-            // frontier degree scan and tiling, then the push or relax kernel
-            if (F <= kSmallFrontier) {
-                launch(ctx, "k_scan_small", k_scan_small<OffT>, 1, kBlock, 0, st, (const uint32_t *)q, d_ctl, off,
-                       (OffT)m, sc, rs);
-            } else {
-                int nb = grid_for(F, kBlock, 1024);
-                launch(ctx, "k_scan_reduce", k_scan_reduce<OffT>, nb, kBlock, 0, st, (const uint32_t *)q,
-                       (const TravCtl *)d_ctl, off, (OffT)m, bsum);
-                launch(ctx, "k_scan_bsums", k_scan_bsums, 1, kBlock, 0, st, bsum, nb, d_ctl);
-                launch(ctx, "k_scan_write", k_scan_write<OffT>, nb, kBlock, 0, st, (const uint32_t *)q,
-                       (const TravCtl *)d_ctl, off, (OffT)m, (const unsigned long long *)bsum, sc, rs);
-            }
-            launch(ctx, "k_tile_rows", k_tile_rows<OffT>, sms * 4, kBlock, 0, st, (const OffT *)sc,
-                   (const TravCtl *)d_ctl, tr);
-            if (weighted) {
-                PTG_CUDA_TRY(cudaMemsetAsync(Mn, 0, n * 8, st));
-                launch(ctx, "k_ms_relax", k_ms_relax<OffT>, sms * 6, kBlock, 0, st, (const uint32_t *)q,
-                       (const OffT *)sc, (const OffT *)rs, (const uint32_t *)tr, col, wt, dist, (const u64 *)Mc,
-                       Mn, (const TravCtl *)d_ctl);
-                launch(ctx, "k_ms_queue", k_ms_queue<OffT>, vgrid, kBlock, 0, st, (const u64 *)Mn, n, off, qn,
-                       d_ctl);
-            } else {
-                PTG_CUDA_TRY(cudaMemsetAsync(Mn, 0, n * 8, st));
-                launch(ctx, "k_ms_push", k_ms_push<OffT>, sms * 8, kBlock, 0, st, (const uint32_t *)q,
-                       (const OffT *)sc, (const OffT *)rs, (const uint32_t *)tr, col, (const u64 *)Mc,
-                       (const u64 *)S, Mn, (const TravCtl *)d_ctl);
-                launch(ctx, "k_ms_update", k_ms_update<OffT>, vgrid, kBlock, 0, st, n, off, Mn, S, d_rows,
-                       level + 1, qn, d_ctl);
-            }
-        }
+        ms_scan<OffT>(ctx, ws, off, m, F, d_ctl);
+        PTG_CUDA_TRY(cudaMemsetAsync(Mn, 0, n * 8, st));
+        launch(ctx, "k_mss_relax", k_mss_relax<OffT>, sms * 6, kBlock, 0, st, (const uint32_t *)ws.q[0].p,
+               (const OffT *)ws.scan.p, (const OffT *)ws.rowstart.p, (const uint32_t *)ws.tiles.p, col, wt, dist,
+               (const u64 *)Mc, Mn, (const TravCtl *)d_ctl);
+        launch(ctx, "k_msb_queue", k_msb_queue<OffT, 1>, vgrid, kBlock, 0, st, (const u64 *)Mn, n, off,
+               ws.q[1].as<uint32_t>(), d_ctl);
         PTG_CUDA_TRY(cudaGetLastError());
-        PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
-        PTG_CUDA_TRY(cudaStreamSynchronize(st));
-        PTG_REQUIRE(h_ctl->error == 0, PTG_ERR_CUDA, "frontier overflow in multi-source round");
-        rr.edges_relaxed += pull ? 0 : h_ctl->E;
-        F = h_ctl->next_tail;
-        Eact = h_ctl->m_unvisited;
-        std::swap(ws.q[0].p, ws.q[1].p);
-        std::swap(ws.q[0].bytes, ws.q[1].bytes);
-        q = ws.q[0].as<uint32_t>();
+        ms_next(ctx, ws, F, Eact, E);
+        rr.edges_relaxed += E;
         cur ^= 1;
-        level++;
     }
-    if (weighted)
-        launch(ctx, "k_ms_transpose", k_ms_transpose, grid_for((n + 31) / 32, 1, sms * 8), kBlock, 0, st,
-               (const uint32_t *)dist, n, k, d_rows);
+    launch(ctx, "k_mss_transpose", k_mss_transpose, grid_for((n + 31) / 32, 1, sms * 8), kBlock, 0, st,
+           (const uint32_t *)dist, n, k, d_rows);
     PTG_CUDA_TRY(cudaGetLastError());
+    (void)Eact;
 }
 
 }  // namespace
 
-// One group of at most 64 sources; d_rows receives k rows of n values.
-// Returns false when the fused path does not apply (out-of-core graphs).
+// Sources per fused group: 256 for BFS (4 mask words), 64 for SSSP.
+uint32_t ms_group_size(bool weighted) { return weighted ? 64u : 256u; }
+
+// One group of at most ms_group_size() sources; d_rows receives k rows of n
+// values.  Returns false when the fused path does not apply (out-of-core).
 bool ms_group(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_rows, bool weighted,
               uint32_t flags, RunResult &rr) {
-    if (g->out_of_core || k == 0 || k > 64) return false;
-    if (g->off64) ms_group_impl<unsigned long long>(g, h_srcs, k, d_rows, weighted, flags, rr);
-    else ms_group_impl<uint32_t>(g, h_srcs, k, d_rows, weighted, flags, rr);
+    if (g->out_of_core || k == 0 || k > ms_group_size(weighted)) return false;
+    bool o64 = g->off64;
+    if (weighted) {
+        if (o64) mssssp_impl<unsigned long long>(g, h_srcs, k, d_rows, flags, rr);
+        else mssssp_impl<uint32_t>(g, h_srcs, k, d_rows, flags, rr);
+    } else if (k <= 64) {
+        if (o64) msbfs_impl<unsigned long long, 1>(g, h_srcs, k, d_rows, flags, rr);
+        else msbfs_impl<uint32_t, 1>(g, h_srcs, k, d_rows, flags, rr);
+    } else if (k <= 128) {
+        if (o64) msbfs_impl<unsigned long long, 2>(g, h_srcs, k, d_rows, flags, rr);
+        else msbfs_impl<uint32_t, 2>(g, h_srcs, k, d_rows, flags, rr);
+    } else {
+        if (o64) msbfs_impl<unsigned long long, 4>(g, h_srcs, k, d_rows, flags, rr);
+        else msbfs_impl<uint32_t, 4>(g, h_srcs, k, d_rows, flags, rr);
+    }
     return true;
 }
 
