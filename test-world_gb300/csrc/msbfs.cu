@@ -121,10 +121,38 @@ __global__ void __launch_bounds__(kBlock) k_msb_push(const uint32_t *q, const Of
     }
 }
 
+// Load a vertex's W mask words (16-byte vector loads for W >= 2).
+template <int W>
+__device__ __forceinline__ void load_mask(const u64 *p, u64 (&x)[W]) {
+    if (W == 1) {
+        x[0] = p[0];
+    } else {
+#pragma unroll
+        for (int i = 0; i < W / 2; i++) {
+            ulonglong2 t = reinterpret_cast<const ulonglong2 *>(p)[i];
+            x[2 * i] = t.x;
+            x[2 * i + 1] = t.y;
+        }
+    }
+}
+
+// OR the warp's new masks into the next level's live-source mask.
+template <int W>
+__device__ __forceinline__ void live_or(u64 *live_next, const u64 (&nb)[W]) {
+#pragma unroll
+    for (int w = 0; w < W; w++) {
+        u64 x = nb[w];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x |= __shfl_xor_sync(0xffffffffu, x, o);
+        if (lane_id() == 0 && x) atomicOr(&live_next[w], x);
+    }
+}
+
 // After a push: N[v] &= ~S[v], S |= N, levels written, next queue built.
 template <class OffT, int W>
 __global__ void __launch_bounds__(kBlock) k_msb_update(uint64_t n, const OffT *off, u64 *N, u64 *S,
-                                                       uint32_t *out, uint32_t val, uint32_t *q, TravCtl *ctl) {
+                                                       uint32_t *out, uint32_t val, uint32_t *q, TravCtl *ctl,
+                                                       u64 *live_next) {
     unsigned long long degsum = 0;
     uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     uint64_t span = (n + 31) / 32 * 32;
@@ -147,6 +175,7 @@ __global__ void __launch_bounds__(kBlock) k_msb_update(uint64_t n, const OffT *o
             any |= nb[w] != 0ull;
         }
         msb_write_levels<W>(out, n, v, valid, nb, val);
+        live_or<W>(live_next, nb);
         if (any) {
             degsum += (unsigned long long)(off[v + 1] - off[v]);
             warp_append(q, &ctl->next_tail, (unsigned)n, &ctl->error, (uint32_t)v);
@@ -156,17 +185,21 @@ __global__ void __launch_bounds__(kBlock) k_msb_update(uint64_t n, const OffT *o
     if (threadIdx.x == 0 && degsum) atomicAdd(&ctl->m_unvisited, degsum);
 }
 
-// Pull level (symmetric graphs): N[v] = (OR of F over v's neighbours) & ~S[v],
-// stopping early once every source has seen v.  A neighbour's W words are one
-// 32-byte sector for W = 4.
+// Pull level (symmetric graphs): N[v] = (OR of F over v's neighbours) & ~S[v].
+// A vertex can only gain sources that are live (in some frontier mask this
+// level), so it stops as soon as it holds all live sources it has not seen;
+// sources whose search died out (small components) no longer keep hubs
+// scanning their whole adjacency.  A neighbour's W words are one 32-byte
+// sector for W = 4, read with 16-byte vector loads.
 template <class OffT, int W>
 __global__ void __launch_bounds__(kBlock) k_msb_pull(uint64_t n, const OffT *off, const uint32_t *col,
-                                                     const u64 *F, u64 *S, u64 *N, const u64 *all_words,
-                                                     uint32_t *out, uint32_t val, uint32_t *q, TravCtl *ctl) {
+                                                     const u64 *F, u64 *S, u64 *N, const u64 *live_in,
+                                                     uint32_t *out, uint32_t val, uint32_t *q, TravCtl *ctl,
+                                                     u64 *live_next) {
     unsigned long long degsum = 0;
-    u64 all[W];
+    u64 live[W];
 #pragma unroll
-    for (int w = 0; w < W; w++) all[w] = all_words[w];
+    for (int w = 0; w < W; w++) live[w] = live_in[w];
     uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     uint64_t span = (n + 31) / 32 * 32;
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < span; v += stride) {
@@ -176,14 +209,15 @@ __global__ void __launch_bounds__(kBlock) k_msb_pull(uint64_t n, const OffT *off
 #pragma unroll
         for (int w = 0; w < W; w++) nb[w] = 0;
         if (valid) {
-            u64 s[W];
-            bool full = true;
+            u64 s[W], need[W];
+            load_mask<W>(S + v * W, s);
+            bool none = true;
 #pragma unroll
             for (int w = 0; w < W; w++) {
-                s[w] = S[v * W + w];
-                full &= s[w] == all[w];
+                need[w] = live[w] & ~s[w];
+                none &= need[w] == 0ull;
             }
-            if (!full) {
+            if (!none) {
                 OffT b = off[v], e = off[v + 1];
                 u64 acc[W];
 #pragma unroll
@@ -191,11 +225,14 @@ __global__ void __launch_bounds__(kBlock) k_msb_pull(uint64_t n, const OffT *off
                 for (OffT k = b; k < e; k += 2) {
                     uint32_t c0 = col[k];
                     uint32_t c1 = k + 1 < e ? col[k + 1] : c0;
+                    u64 f0[W], f1[W];
+                    load_mask<W>(F + (uint64_t)c0 * W, f0);
+                    load_mask<W>(F + (uint64_t)c1 * W, f1);
                     bool done = true;
 #pragma unroll
                     for (int w = 0; w < W; w++) {
-                        acc[w] |= F[(uint64_t)c0 * W + w] | F[(uint64_t)c1 * W + w];
-                        done &= (acc[w] | s[w]) == all[w];
+                        acc[w] |= f0[w] | f1[w];
+                        done &= (acc[w] & need[w]) == need[w];
                     }
                     if (done) break;
                 }
@@ -210,6 +247,7 @@ __global__ void __launch_bounds__(kBlock) k_msb_pull(uint64_t n, const OffT *off
             for (int w = 0; w < W; w++) N[v * W + w] = nb[w];
         }
         msb_write_levels<W>(out, n, v, valid, nb, val);
+        live_or<W>(live_next, nb);
         if (any) {
             degsum += (unsigned long long)(off[v + 1] - off[v]);
             warp_append(q, &ctl->next_tail, (unsigned)n, &ctl->error, (uint32_t)v);
@@ -380,7 +418,8 @@ void ms_prepare(ptg_graph *g, uint64_t mask_bytes) {
     ws.scan.ensure((n + 1) * sizeof(OffT));
     ws.rowstart.ensure((n + 1) * sizeof(OffT));
     ws.tiles.ensure((m / kTile + 4) * 4);
-    ws.bsum.ensure(1024 * 8 + 256 * 4 + 64);
+    // scan partials | 256 sources | all-sources mask | two live-source masks
+    ws.bsum.ensure(1024 * 8 + 256 * 4 + 3 * 32);
     ws.ctl.ensure(sizeof(TravCtl));
     ws.h_ctl.ensure(sizeof(TravCtl));
 }
@@ -439,15 +478,20 @@ void msbfs_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_ro
     ms_next(ctx, ws, F, Eact, E);
     uint32_t level = base;
     int cur = 0;
+    // live[c]: OR of every frontier mask of the current level (the sources
+    // still expanding); the seed frontier holds all of them.
+    u64 *d_live[2] = {d_all + 4, d_all + 8};
+    PTG_CUDA_TRY(cudaMemcpyAsync(d_live[0], all, sizeof(all), cudaMemcpyHostToDevice, st));
     const uint32_t max_rounds = (uint32_t)std::min<uint64_t>(0xFFFFFFF0ull, n + 16);
     while (F > 0) {
         if (rr.iterations >= max_rounds) throw Error{PTG_ERR_TIMEOUT, "iteration limit reached"};
         rr.iterations++;
         u64 *Mc = cur ? M1 : M0, *Mn = cur ? M0 : M1;
+        PTG_CUDA_TRY(cudaMemsetAsync(d_live[cur ^ 1], 0, 8 * W, st));
         bool pull = g->symmetric && Eact * 10 > m;
         if (pull) {
             launch(ctx, "k_msb_pull", k_msb_pull<OffT, W>, vgrid, kBlock, 0, st, n, off, col, (const u64 *)Mc, S, Mn,
-                   (const u64 *)d_all, d_rows, level + 1, ws.q[1].as<uint32_t>(), d_ctl);
+                   (const u64 *)d_live[cur], d_rows, level + 1, ws.q[1].as<uint32_t>(), d_ctl, d_live[cur ^ 1]);
         } else {
             ms_scan<OffT>(ctx, ws, off, m, F, d_ctl);
             PTG_CUDA_TRY(cudaMemsetAsync(Mn, 0, n * 8 * W, st));
@@ -455,7 +499,7 @@ void msbfs_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_ro
                    (const OffT *)ws.scan.p, (const OffT *)ws.rowstart.p, (const uint32_t *)ws.tiles.p, col,
                    (const u64 *)Mc, (const u64 *)S, Mn, (const TravCtl *)d_ctl);
             launch(ctx, "k_msb_update", k_msb_update<OffT, W>, vgrid, kBlock, 0, st, n, off, Mn, S, d_rows,
-                   level + 1, ws.q[1].as<uint32_t>(), d_ctl);
+                   level + 1, ws.q[1].as<uint32_t>(), d_ctl, d_live[cur ^ 1]);
         }
         PTG_CUDA_TRY(cudaGetLastError());
         ms_next(ctx, ws, F, Eact, E);

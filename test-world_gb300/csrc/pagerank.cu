@@ -149,7 +149,7 @@ __device__ __forceinline__ void finalize_row(const PrArgs &a, const PrConst &c, 
 }
 
 template <class OffT>
-__global__ void __launch_bounds__(kBlock) k_spmv(PrArgs a) {
+__global__ void __launch_bounds__(kBlock, 8) k_spmv(PrArgs a) {
     __shared__ OffT s_end[kPrTile + 1];   // row ends of the CTA's rows
     __shared__ float s_val[kPrTile + 1];  // gathered contributions of its edges
     __shared__ uint32_t s_key[kBlock];    // carry row per thread (local index)
