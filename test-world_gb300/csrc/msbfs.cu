@@ -185,76 +185,136 @@ __global__ void __launch_bounds__(kBlock) k_msb_update(uint64_t n, const OffT *o
     if (threadIdx.x == 0 && degsum) atomicAdd(&ctl->m_unvisited, degsum);
 }
 
-// Pull level (symmetric graphs): N[v] = (OR of F over v's neighbours) & ~S[v].
-// A vertex can only gain sources that are live (in some frontier mask this
-// level), so it stops as soon as it holds all live sources it has not seen;
-// sources whose search died out (small components) no longer keep hubs
-// scanning their whole adjacency.  A neighbour's W words are one 32-byte
-// sector for W = 4, read with 16-byte vector loads.
+// Pull level (symmetric graphs): N[v] = (OR of F over v's neighbours) & ~S[v],
+// followed by k_msb_update.  A vertex can only gain sources that are live (in
+// some frontier mask this level), so its scan stops as soon as it holds all
+// live sources it has not seen; sources whose search died out (small
+// components) no longer keep hubs scanning.  Work is split by degree so that
+// no thread walks a long adjacency alone: vertices of degree <= kPullSmall
+// are one thread each (k_msb_pull_small); the adjacency of every other vertex
+// is cut into kPullChunk-edge work items, one warp each (k_msb_pull_big),
+// whose partial masks meet in N through atomicOr.  A neighbour's W words are
+// one 32-byte sector for W = 4, read with 16-byte vector loads.
+constexpr uint32_t kPullSmall = 32;
+constexpr uint32_t kPullChunk = 1024;
+
+// Work items (vertex, chunk) of the vertices above kPullSmall; counted first
+// (items == nullptr), then written.  Item order is irrelevant.
+template <class OffT>
+__global__ void k_pull_items(uint64_t n, const OffT *off, uint2 *items, unsigned long long *count) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t deg = (uint64_t)(off[v + 1] - off[v]);
+        if (deg <= kPullSmall) continue;
+        uint32_t c = (uint32_t)((deg + kPullChunk - 1) / kPullChunk);
+        unsigned long long base = atomicAdd(count, (unsigned long long)c);
+        if (items)
+            for (uint32_t i = 0; i < c; i++) items[base + i] = make_uint2((uint32_t)v, i);
+    }
+}
+
 template <class OffT, int W>
-__global__ void __launch_bounds__(kBlock) k_msb_pull(uint64_t n, const OffT *off, const uint32_t *col,
-                                                     const u64 *F, u64 *S, u64 *N, const u64 *live_in,
-                                                     uint32_t *out, uint32_t val, uint32_t *q, TravCtl *ctl,
-                                                     u64 *live_next) {
-    unsigned long long degsum = 0;
+__global__ void __launch_bounds__(kBlock) k_msb_pull_small(uint64_t n, const OffT *off, const uint32_t *col,
+                                                           const u64 *F, const u64 *S, u64 *N,
+                                                           const u64 *live_in) {
     u64 live[W];
 #pragma unroll
     for (int w = 0; w < W; w++) live[w] = live_in[w];
-    uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    uint64_t span = (n + 31) / 32 * 32;
-    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < span; v += stride) {
-        bool valid = v < n;
-        u64 nb[W];
-        bool any = false;
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
+        OffT b = off[v], e = off[v + 1];
+        if (b == e || (uint64_t)(e - b) > kPullSmall) continue;
+        u64 s[W], need[W];
+        load_mask<W>(S + v * W, s);
+        bool none = true;
 #pragma unroll
-        for (int w = 0; w < W; w++) nb[w] = 0;
-        if (valid) {
-            u64 s[W], need[W];
-            load_mask<W>(S + v * W, s);
-            bool none = true;
+        for (int w = 0; w < W; w++) {
+            need[w] = live[w] & ~s[w];
+            none &= need[w] == 0ull;
+        }
+        if (none) continue;
+        u64 acc[W];
+#pragma unroll
+        for (int w = 0; w < W; w++) acc[w] = 0;
+        for (OffT k = b; k < e; k += 2) {
+            uint32_t c0 = col[k];
+            uint32_t c1 = k + 1 < e ? col[k + 1] : c0;
+            u64 f0[W], f1[W];
+            load_mask<W>(F + (uint64_t)c0 * W, f0);
+            load_mask<W>(F + (uint64_t)c1 * W, f1);
+            bool done = true;
 #pragma unroll
             for (int w = 0; w < W; w++) {
-                need[w] = live[w] & ~s[w];
-                none &= need[w] == 0ull;
+                acc[w] |= f0[w] | f1[w];
+                done &= (acc[w] & need[w]) == need[w];
             }
-            if (!none) {
-                OffT b = off[v], e = off[v + 1];
-                u64 acc[W];
-#pragma unroll
-                for (int w = 0; w < W; w++) acc[w] = 0;
-                for (OffT k = b; k < e; k += 2) {
-                    uint32_t c0 = col[k];
-                    uint32_t c1 = k + 1 < e ? col[k + 1] : c0;
-                    u64 f0[W], f1[W];
-                    load_mask<W>(F + (uint64_t)c0 * W, f0);
-                    load_mask<W>(F + (uint64_t)c1 * W, f1);
-                    bool done = true;
-#pragma unroll
-                    for (int w = 0; w < W; w++) {
-                        acc[w] |= f0[w] | f1[w];
-                        done &= (acc[w] & need[w]) == need[w];
-                    }
-                    if (done) break;
-                }
-#pragma unroll
-                for (int w = 0; w < W; w++) {
-                    nb[w] = acc[w] & ~s[w];
-                    if (nb[w]) S[v * W + w] = s[w] | nb[w];
-                    any |= nb[w] != 0ull;
-                }
-            }
-#pragma unroll
-            for (int w = 0; w < W; w++) N[v * W + w] = nb[w];
+            if (done) break;
         }
-        msb_write_levels<W>(out, n, v, valid, nb, val);
-        live_or<W>(live_next, nb);
-        if (any) {
-            degsum += (unsigned long long)(off[v + 1] - off[v]);
-            warp_append(q, &ctl->next_tail, (unsigned)n, &ctl->error, (uint32_t)v);
+#pragma unroll
+        for (int w = 0; w < W; w++)
+            if (acc[w] & need[w]) N[v * W + w] = acc[w] & need[w];
+    }
+}
+
+template <class OffT, int W>
+__global__ void __launch_bounds__(kBlock) k_msb_pull_big(const uint2 *items, uint64_t nitems, const OffT *off,
+                                                         const uint32_t *col, const u64 *F, const u64 *S, u64 *N,
+                                                         const u64 *live_in) {
+    constexpr int kU = 4;  // column loads in flight per lane
+    u64 live[W];
+#pragma unroll
+    for (int w = 0; w < W; w++) live[w] = live_in[w];
+    const int lane = (int)lane_id();
+    const uint64_t nwarps = (uint64_t)gridDim.x * blockDim.x / 32;
+    for (uint64_t it = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; it < nitems; it += nwarps) {
+        uint2 item = items[it];
+        uint64_t v = item.x;
+        u64 s[W], need[W];
+        load_mask<W>(S + v * W, s);
+        bool none = true;
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+            need[w] = live[w] & ~s[w];
+            none &= need[w] == 0ull;
+        }
+        if (none) continue;  // warp-uniform: every lane read the same words
+        OffT b = off[v] + (OffT)item.y * (OffT)kPullChunk;
+        OffT e = off[v + 1];
+        if (e - b > (OffT)kPullChunk) e = b + (OffT)kPullChunk;
+        u64 acc[W];
+#pragma unroll
+        for (int w = 0; w < W; w++) acc[w] = 0;
+        for (OffT k0 = b; k0 < e; k0 += 32 * kU) {
+            uint32_t c[kU];
+#pragma unroll
+            for (int j = 0; j < kU; j++) {
+                OffT k = k0 + (OffT)(j * 32 + lane);
+                c[j] = k < e ? col[k] : 0u;
+            }
+#pragma unroll
+            for (int j = 0; j < kU; j++) {
+                if (k0 + (OffT)(j * 32 + lane) < e) {
+                    u64 f[W];
+                    load_mask<W>(F + (uint64_t)c[j] * W, f);
+#pragma unroll
+                    for (int w = 0; w < W; w++) acc[w] |= f[w];
+                }
+            }
+            bool done = true;
+#pragma unroll
+            for (int w = 0; w < W; w++) {
+                u64 x = acc[w];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) x |= __shfl_xor_sync(0xffffffffu, x, o);
+                acc[w] = x;
+                done &= (x & need[w]) == need[w];
+            }
+            if (done) break;  // warp-uniform after the all-reduce
+        }
+#pragma unroll
+        for (int w = 0; w < W; w++) {
+            u64 x = acc[w] & need[w];
+            if (lane == w && x) atomicOr(&N[v * W + w], x);
         }
     }
-    degsum = block_reduce_sum(degsum);
-    if (threadIdx.x == 0 && degsum) atomicAdd(&ctl->m_unvisited, degsum);
 }
 
 // ---------------------------------------------------------------------------
@@ -424,6 +484,29 @@ void ms_prepare(ptg_graph *g, uint64_t mask_bytes) {
     ws.h_ctl.ensure(sizeof(TravCtl));
 }
 
+// Chunked work items of the high-degree vertices, built once per graph.
+template <class OffT>
+void build_pull_items(ptg_graph *g) {
+    ptg_ctx *ctx = g->ctx;
+    cudaStream_t st = ctx->stream;
+    const OffT *off = g->d_off.as<OffT>();
+    unsigned long long *cnt = ctx->ws.bsum.as<unsigned long long>();
+    int grid = grid_for(g->n, kBlock, ctx->sm_count * 8);
+    PTG_CUDA_TRY(cudaMemsetAsync(cnt, 0, 8, st));
+    launch(ctx, "k_pull_items", k_pull_items<OffT>, grid, kBlock, 0, st, g->n, off, (uint2 *)nullptr, cnt);
+    unsigned long long total = 0;
+    PTG_CUDA_TRY(cudaMemcpyAsync(&total, cnt, 8, cudaMemcpyDeviceToHost, st));
+    PTG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (total) {
+        g->d_pull_items.ensure(total * sizeof(uint2));
+        PTG_CUDA_TRY(cudaMemsetAsync(cnt, 0, 8, st));
+        launch(ctx, "k_pull_items", k_pull_items<OffT>, grid, kBlock, 0, st, g->n, off,
+               g->d_pull_items.as<uint2>(), cnt);
+    }
+    g->n_pull_items = total;
+    g->pull_items_built = true;
+}
+
 // Read back the control block, take the new queue, reset counters.
 inline void ms_next(ptg_ctx *ctx, Workspace &ws, uint64_t &F, uint64_t &Eact, uint64_t &E) {
     cudaStream_t st = ctx->stream;
@@ -452,6 +535,7 @@ void msbfs_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_ro
     const uint32_t *col = g->d_col.as<uint32_t>();
     uint32_t base = (flags & PTG_LEVEL_ZERO_BASED) ? 0u : 1u;
     ms_prepare<OffT>(g, n * 8 * W);
+    if (g->symmetric && !g->pull_items_built) build_pull_items<OffT>(g);
     u64 *M0 = ws.ms[0].as<u64>(), *M1 = ws.ms[1].as<u64>(), *S = ws.ms[2].as<u64>();
     unsigned long long *bsum = ws.bsum.as<unsigned long long>();
     uint32_t *d_srcs = reinterpret_cast<uint32_t *>(bsum + 1024);
@@ -489,18 +573,22 @@ void msbfs_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_ro
         u64 *Mc = cur ? M1 : M0, *Mn = cur ? M0 : M1;
         PTG_CUDA_TRY(cudaMemsetAsync(d_live[cur ^ 1], 0, 8 * W, st));
         bool pull = g->symmetric && Eact * 10 > m;
+        PTG_CUDA_TRY(cudaMemsetAsync(Mn, 0, n * 8 * W, st));
         if (pull) {
-            launch(ctx, "k_msb_pull", k_msb_pull<OffT, W>, vgrid, kBlock, 0, st, n, off, col, (const u64 *)Mc, S, Mn,
-                   (const u64 *)d_live[cur], d_rows, level + 1, ws.q[1].as<uint32_t>(), d_ctl, d_live[cur ^ 1]);
+            launch(ctx, "k_msb_pull_small", k_msb_pull_small<OffT, W>, vgrid, kBlock, 0, st, n, off, col,
+                   (const u64 *)Mc, (const u64 *)S, Mn, (const u64 *)d_live[cur]);
+            if (g->n_pull_items)
+                launch(ctx, "k_msb_pull_big", k_msb_pull_big<OffT, W>, sms * 8, kBlock, 0, st,
+                       (const uint2 *)g->d_pull_items.p, g->n_pull_items, off, col, (const u64 *)Mc,
+                       (const u64 *)S, Mn, (const u64 *)d_live[cur]);
         } else {
             ms_scan<OffT>(ctx, ws, off, m, F, d_ctl);
-            PTG_CUDA_TRY(cudaMemsetAsync(Mn, 0, n * 8 * W, st));
             launch(ctx, "k_msb_push", k_msb_push<OffT, W>, sms * 8, kBlock, 0, st, (const uint32_t *)ws.q[0].p,
                    (const OffT *)ws.scan.p, (const OffT *)ws.rowstart.p, (const uint32_t *)ws.tiles.p, col,
                    (const u64 *)Mc, (const u64 *)S, Mn, (const TravCtl *)d_ctl);
-            launch(ctx, "k_msb_update", k_msb_update<OffT, W>, vgrid, kBlock, 0, st, n, off, Mn, S, d_rows,
-                   level + 1, ws.q[1].as<uint32_t>(), d_ctl, d_live[cur ^ 1]);
         }
+        launch(ctx, "k_msb_update", k_msb_update<OffT, W>, vgrid, kBlock, 0, st, n, off, Mn, S, d_rows,
+               level + 1, ws.q[1].as<uint32_t>(), d_ctl, d_live[cur ^ 1]);
         PTG_CUDA_TRY(cudaGetLastError());
         ms_next(ctx, ws, F, Eact, E);
         rr.edges_relaxed += pull ? 0 : E;

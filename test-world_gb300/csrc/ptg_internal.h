@@ -234,6 +234,9 @@ struct ptg_graph {
     ptg::DevBuf d_tiles;  // merge-path tile table (PageRank, CC), built on first use
     ptg::DevBuf d_nzbm;   // bitmap of vertices with edges (bottom-up BFS), built on first use
     double mean_weight = 0;  // mean resident edge weight (SSSP bucket width), measured on first use
+    ptg::DevBuf d_pull_items;  // (vertex, chunk) work items of high-degree vertices (multi-source pull)
+    uint64_t n_pull_items = 0;
+    bool pull_items_built = false;
     // out-of-core
     bool out_of_core = false;
     uint64_t resident_edges = 0;
