@@ -46,9 +46,16 @@ def parse():
     p.add_argument("--sssp-sources", type=int, default=4)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--workload", default="suite", choices=["suite", "batch"],
+    p.add_argument("--workload", default="suite", choices=["suite", "batch", "serve"],
                    help="suite: the in-HBM suite on RMAT-24 (default); batch: 1024-source MS-BFS/MS-SSSP "
-                        "on RMAT-22 and CC over a batch of ER graphs, each against one-at-a-time calls")
+                        "on RMAT-22 and CC over a batch of ER graphs, each against one-at-a-time calls; "
+                        "serve: a Poisson stream of BFS/SSSP/PPR requests through the server")
+    p.add_argument("--serve-scale", type=int, default=26)
+    p.add_argument("--serve-uploads", type=int, default=16)
+    p.add_argument("--serve-requests", type=int, default=4000)
+    p.add_argument("--serve-rate", type=float, default=2000.0)
+    p.add_argument("--serve-lanes", type=int, default=4)
+    p.add_argument("--plain-sample", type=int, default=240)
     p.add_argument("--er-graphs", type=int, default=4096)
     p.add_argument("--batch-sources", type=int, default=1024)
     p.add_argument("--profile-case", action="store_true",
@@ -135,6 +142,152 @@ def batch_workload(args):
                        "plain_sample": psample, "gen_s": gen_s,
                        "note": "device time of the kernels; plain = one ptg_cc launch sequence per graph"}
     print(json.dumps({"workload": "batched", "metric": "batched_queries_per_s", "results": res}))
+
+
+def serve_workload(args):
+    """Serving: a seeded Poisson stream (rate --serve-rate) of BFS 50% / SSSP 30% /
+    PPR 20% (FP32, 20 iterations) requests over a resident RMAT graph of scale
+    --serve-scale and --serve-uploads uploaded RMAT graphs of scales 10..20, all
+    admitted through the server's memory budget.  Each request picks its graph
+    uniformly and a random non-isolated source; results are copied to pinned host
+    buffers.  Latency = completion - scheduled arrival.  The plain method (one
+    query at a time through ptg_bfs/ptg_sssp/ptg_ppr, host outputs) is timed on
+    the first --plain-sample requests of the same stream; its throughput is the
+    sample's count / summed service time, and its latencies follow from a FIFO
+    single-server queue (Lindley's recursion) fed the same arrivals with the
+    measured service times of each request's (graph, kind) class."""
+    import queue
+    import torch
+    import ptgraph
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    ctx = ptgraph.Ctx(local)
+    rng = np.random.default_rng(2000)
+    t0 = time.time()
+    graphs = [ptgraph.gen_rmat(args.serve_scale, 16, 0.57, 0.19, 0.19, seed=5, symmetric=True, wmin=1, wmax=63)]
+    scales = [10 + (10 * i) // max(1, args.serve_uploads - 1) for i in range(args.serve_uploads)]
+    for i, sc in enumerate(scales):
+        graphs.append(ptgraph.gen_rmat(sc, 16, 0.57, 0.19, 0.19, seed=100 + i, symmetric=True, wmin=1, wmax=63))
+    gen_s = time.time() - t0
+    nz = [np.nonzero(np.diff(off.astype(np.int64)))[0].astype(np.uint32) for off, _, _ in graphs]
+    N = args.serve_requests
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, N))
+    kinds = rng.choice(3, N, p=[0.5, 0.3, 0.2])
+    gidx = rng.integers(0, len(graphs), N)
+    srcs = np.array([nz[g][rng.integers(nz[g].size)] for g in gidx], dtype=np.uint32)
+
+    srv = ptgraph.Server(ctx, lanes=args.serve_lanes)
+    t0 = time.time()
+    up = [srv.upload(off, col, w) for off, col, w in graphs]
+    upload_s = time.time() - t0
+    gids = [g for g, _ in up]
+    # pinned result pools per graph (a request takes a buffer, its waiter returns it)
+    pools = []
+    for off, _, _ in graphs:
+        n = off.size - 1
+        q = queue.Queue()
+        for _ in range(64 if n > (1 << 22) else 128):
+            q.put(torch.empty(n, dtype=torch.int32, pin_memory=True))
+        pools.append(q)
+    keep = {}  # copies of a few results for the identity check against the plain path
+    done_t = np.zeros(N)
+    sub_t = np.zeros(N)
+    lat_srv = np.zeros(N)
+    work = queue.Queue()
+
+    def waiter():
+        while True:
+            item = work.get()
+            if item is None:
+                return
+            i, rid, buf = item
+            _, lat = srv.wait(rid)
+            lat_srv[i] = lat * 1e-6
+            if i < 48:
+                keep[i] = buf.numpy().copy()
+            pools[gidx[i]].put(buf)
+
+    waiters = [threading.Thread(target=waiter) for _ in range(8)]
+    for t in waiters:
+        t.start()
+    start = time.perf_counter()
+    for i in range(N):
+        delay = start + arrivals[i] - time.perf_counter()
+        if delay > 0:
+            time.sleep(delay)
+        buf = pools[gidx[i]].get()
+        sub_t[i] = time.perf_counter() - start
+        rid = srv.submit(gids[gidx[i]], int(kinds[i]), int(srcs[i]), out=buf)
+        work.put((i, rid, buf))
+    for _ in waiters:
+        work.put(None)
+    for t in waiters:
+        t.join()
+    srv_stats = srv.stats()
+    srv.close()
+    lat = (sub_t - arrivals) + lat_srv
+    done_t = sub_t + lat_srv
+    makespan = done_t.max() - arrivals[0]
+    names = ["bfs", "sssp", "ppr"]
+    big = gidx == 0
+
+    def pct(x):
+        return {"p50_ms": float(np.percentile(x, 50) * 1e3), "p99_ms": float(np.percentile(x, 99) * 1e3),
+                "count": int(x.size)} if x.size else None
+
+    res = {"requests": N, "offered_rate": args.serve_rate, "qps": N / makespan, "makespan_s": makespan,
+           **{k: v for k, v in pct(lat).items() if k != "count"},
+           "by_kind": {names[k]: pct(lat[kinds == k]) for k in range(3)},
+           "resident_graph": pct(lat[big]), "uploaded_graphs": pct(lat[~big]),
+           "server": {k: srv_stats[k] for k in ("batches", "max_batch_seen", "failed", "launches",
+                                                 "resident_graphs", "streamed_graphs", "budget_bytes",
+                                                 "committed_bytes", "busy_ms")},
+           "lanes": args.serve_lanes, "graphs": {"resident_scale": args.serve_scale, "upload_scales": scales,
+                                                 "admitted_resident": [bool(r) for _, r in up]},
+           "gen_s": gen_s, "upload_s": upload_s}
+    # plain: one query at a time, same requests, host outputs
+    G = {}
+    svc = np.zeros(min(args.plain_sample, N))
+    for i in range(svc.size):
+        g = int(gidx[i])
+        if g not in G:
+            off, col, w = graphs[g]
+            G[g] = ctx.graph(off, col, w, symmetric=True)
+        out = torch.empty(G[g].n, dtype=torch.int32, pin_memory=True)
+        o = out.numpy()
+        t = time.perf_counter()
+        if kinds[i] == 0:
+            G[g].bfs(int(srcs[i]), out=o)
+        elif kinds[i] == 1:
+            G[g].sssp(int(srcs[i]), out=o)
+        else:
+            G[g].ppr(int(srcs[i]), out=o.view(np.float32))
+        svc[i] = time.perf_counter() - t
+        if i in keep:
+            assert np.array_equal(keep[i], o) if kinds[i] != 2 else \
+                np.allclose(keep[i].view(np.float32), o.view(np.float32), rtol=2e-6, atol=0), i
+    for h in G.values():
+        h.close()
+    cls_mean = {}
+    for i in range(svc.size):
+        cls_mean.setdefault((int(gidx[i]), int(kinds[i])), []).append(svc[i])
+    cls_mean = {k: float(np.mean(v)) for k, v in cls_mean.items()}
+    kind_mean = {k: float(np.mean(svc[kinds[:svc.size] == k])) for k in range(3)}
+    est = np.array([cls_mean.get((int(gidx[i]), int(kinds[i])), kind_mean[int(kinds[i])]) for i in range(N)])
+    fin = np.zeros(N)
+    free_at = 0.0
+    for i in range(N):
+        st_i = max(arrivals[i], free_at)
+        free_at = st_i + est[i]
+        fin[i] = free_at
+    plat = fin - arrivals
+    plain_qps = svc.size / svc.sum()
+    res["plain"] = {"qps": plain_qps, "sample": int(svc.size), "mean_service_ms": float(svc.mean() * 1e3),
+                    "p50_ms_simulated": float(np.percentile(plat, 50) * 1e3),
+                    "p99_ms_simulated": float(np.percentile(plat, 99) * 1e3)}
+    res["speedup_qps"] = res["qps"] / plain_qps
+    res["identical_results_checked"] = len([i for i in keep if i < svc.size])
+    print(json.dumps({"workload": "serve", "metric": "served_queries_per_s", "results": res}))
 
 
 def multi_dev(G, srcs, out, name, st):
@@ -320,6 +473,9 @@ def main():
         return
     if args.workload == "batch":
         batch_workload(args)
+        return
+    if args.workload == "serve":
+        serve_workload(args)
         return
     import torch
     import ptgraph

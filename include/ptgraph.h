@@ -235,6 +235,12 @@ ptg_status ptg_cc(ptg_graph *g, uint32_t *labels, const ptg_run_opts *opts);
 ptg_status ptg_pagerank(ptg_graph *g, float *rank, const ptg_pr_opts *opts);
 /* Personalized PageRank: teleport (and dangling mass) to src, r0 = e_src. */
 ptg_status ptg_ppr(ptg_graph *g, uint32_t src, float *rank, const ptg_pr_opts *opts);
+/* Personalized PageRank for k sources: rank holds k rows of n floats, row i
+ * the PPR of sources[i] (same semantics and tolerance as ptg_ppr; the
+ * per-vertex sums run in a different order).  Sources run 32 per pass, and a
+ * source's result does not depend on which other sources share its pass. */
+ptg_status ptg_ppr_batch(ptg_graph *g, const uint32_t *sources, uint32_t k, float *rank,
+                         const ptg_pr_opts *opts);
 
 /* BFS that allocates nothing.  This entry point has no counterpart in the
  * reference.  It is for callers that can pass device buffers but must not
@@ -289,30 +295,51 @@ typedef struct ptg_server ptg_server;
 enum { PTG_Q_BFS = 0, PTG_Q_SSSP = 1, PTG_Q_PPR = 2 };
 
 typedef struct ptg_server_config {
-    uint32_t max_slots;           /* concurrent queries on the device; 0 = 256          */
-    uint32_t max_batch;           /* sources per fused batch; 0 = 64                    */
-    uint32_t queue_capacity;      /* pending requests before PTG_ERR_BUSY; 0 = 65536    */
-    uint32_t ppr_iterations;      /* 0 = 20                                             */
-    uint64_t memory_budget_bytes; /* 0 = free HBM at start minus 10%                    */
+    uint32_t lanes;               /* worker lanes (thread + stream + workspace); 0 = 4 */
+    uint32_t max_slots;           /* queries on the device at once; 0 = 1024           */
+    uint32_t max_batch;           /* cap on sources per fused pass; 0 = per kind:
+                                     BFS 256, SSSP 64, PPR 32 (1 disables batching)   */
+    uint32_t queue_capacity;      /* queued requests before PTG_ERR_BUSY; 0 = 65536    */
+    uint32_t ppr_iterations;      /* 0 = 20                                            */
+    uint32_t reserved;
+    double ppr_damping;           /* 0 = 0.85                                          */
+    uint64_t memory_budget_bytes; /* graphs + lane workspaces; 0 = free HBM at
+                                     creation minus 10%                                */
 } ptg_server_config;
 
 ptg_status ptg_server_create(ptg_ctx *ctx, const ptg_server_config *cfg, ptg_server **out);
+/* Pending requests complete with PTG_ERR_CANCELLED; running batches finish. */
 void ptg_server_destroy(ptg_server *s);
-/* Register a graph with the server (the server does not own it). */
+/* Register a graph created by the caller on the server's device (not owned;
+ * it must outlive the server). */
 ptg_status ptg_server_add_graph(ptg_server *s, ptg_graph *g, uint32_t *graph_id);
-/* Submit a query; the result buffer (n entries of u32 for BFS/SSSP, float for
- * PPR, host memory) must stay valid until the request completes. */
+/* Upload a graph, admitted by the memory budget: resident in HBM when it fits
+ * in what the budget has left (*resident = 1), else created out-of-core with
+ * that remainder as its device budget (*resident = 0); a streamed graph reads
+ * the caller's col/weight arrays, which must then stay valid until the server
+ * is destroyed.  Streamed graphs serve BFS/SSSP one query at a time. */
+ptg_status ptg_server_upload(ptg_server *s, const ptg_csr *csr, uint32_t *graph_id, uint32_t *resident);
+/* Submit a query (PTG_Q_BFS, PTG_Q_SSSP on a weighted graph, PTG_Q_PPR on a
+ * resident symmetric graph).  result: n entries (u32 levels/distances, float
+ * ranks) in host or device memory, valid until the request completes; values
+ * follow ptg_bfs / ptg_sssp / ptg_ppr with default flags. */
 ptg_status ptg_server_submit(ptg_server *s, uint32_t graph_id, uint32_t kind, uint32_t src,
                              void *result, uint64_t *request_id);
-/* Wait for a request (timeout_ms < 0: forever).  Returns PTG_ERR_TIMEOUT if
- * not done in time; latency_us receives submit->completion time. */
+/* Wait for a request (timeout_ms < 0: forever) and release its id.  Returns
+ * the request's status, or PTG_ERR_TIMEOUT if not done in time (the id stays
+ * valid); latency_us receives the submit-to-completion time. */
 ptg_status ptg_server_wait(ptg_server *s, uint64_t request_id, int64_t timeout_ms,
                            double *latency_us);
+/* Block until nothing is queued or running. */
 ptg_status ptg_server_drain(ptg_server *s);
 
 typedef struct ptg_server_stats {
-    uint64_t submitted, completed, batches, max_batch_seen;
-    double busy_ms;
+    uint64_t submitted, completed, failed, batches, max_batch_seen;
+    uint64_t budget_bytes;    /* memory budget                                   */
+    uint64_t committed_bytes; /* uploaded graphs + lane workspaces               */
+    uint64_t launches;        /* kernels launched by the lanes                    */
+    uint32_t resident_graphs, streamed_graphs;
+    double busy_ms;           /* summed lane time spent on batches                */
 } ptg_server_stats;
 ptg_status ptg_server_stats_get(ptg_server *s, ptg_server_stats *st);
 

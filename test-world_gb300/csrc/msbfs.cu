@@ -654,6 +654,15 @@ void mssssp_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_r
 
 }  // namespace
 
+// Builds the per-graph tables of the fused passes (pull work items) now
+// rather than on first use.
+void ms_prepare_graph(ptg_graph *g) {
+    if (g->out_of_core || !g->symmetric || g->pull_items_built) return;
+    g->ctx->ws.bsum.ensure(1024 * 8 + 256 * 4 + 3 * 32);
+    if (g->off64) build_pull_items<unsigned long long>(g);
+    else build_pull_items<uint32_t>(g);
+}
+
 // Sources per fused group: 256 for BFS (4 mask words), 64 for SSSP.
 uint32_t ms_group_size(bool weighted) { return weighted ? 64u : 256u; }
 

@@ -237,6 +237,9 @@ struct ptg_graph {
     ptg::DevBuf d_pull_items;  // (vertex, chunk) work items of high-degree vertices (multi-source pull)
     uint64_t n_pull_items = 0;
     bool pull_items_built = false;
+    ptg::DevBuf d_ppr_items, d_ppr_longs;  // long-row chunks (multi-source PPR)
+    uint64_t n_ppr_items = 0, n_ppr_longs = 0;
+    bool ppr_items_built = false;
     // out-of-core
     bool out_of_core = false;
     uint64_t resident_edges = 0;

@@ -459,6 +459,33 @@ __global__ void __launch_bounds__(kBlock) k_far_split(uint32_t *far_bm, uint64_t
 // ---------------------------------------------------------------------------
 // host driver
 // ---------------------------------------------------------------------------
+// Mean resident edge weight (the default SSSP bucket width is half of it),
+// measured once per graph.
+void measure_mean_weight(ptg_graph *g) {
+    if (g->mean_weight != 0 || g->resident_edges == 0 || !g->weighted) return;
+    ptg_ctx *ctx = g->ctx;
+    cudaStream_t st = ctx->stream;
+    ctx->ws.bsum.ensure(1024 * 8);
+    unsigned long long *acc = ctx->ws.bsum.as<unsigned long long>();
+    PTG_CUDA_TRY(cudaMemsetAsync(acc, 0, 8, st));
+    launch(ctx, "k_weight_sum", k_weight_sum, grid_for(g->resident_edges, kBlock, ctx->sm_count * 8), kBlock, 0, st,
+           g->d_w.as<uint32_t>(), g->resident_edges, acc);
+    unsigned long long sum = 0;
+    PTG_CUDA_TRY(cudaMemcpyAsync(&sum, acc, 8, cudaMemcpyDeviceToHost, st));
+    PTG_CUDA_TRY(cudaStreamSynchronize(st));
+    g->mean_weight = std::max(1.0, (double)sum / (double)g->resident_edges);
+}
+
+// Bitmap of vertices with at least one edge (bottom-up BFS), built once per graph.
+template <class OffT>
+void build_nonzero_bits(ptg_graph *g) {
+    if (g->d_nzbm.p) return;
+    uint64_t words = (g->n + 31) / 32;
+    g->d_nzbm.ensure(words * 4);
+    launch(g->ctx, "k_nonzero_bits", k_nonzero_bits<OffT>, grid_for(words, kBlock, g->ctx->sm_count * 8), kBlock, 0,
+           g->ctx->stream, g->d_off.as<OffT>(), g->n, g->d_nzbm.as<uint32_t>());
+}
+
 template <class OffT>
 void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value, uint32_t flags,
                    uint32_t delta, uint32_t max_iters, RunResult &rr) {
@@ -510,17 +537,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         if (use_far) {
             if (delta == 0) {
                 // default bucket width: half the mean edge weight (measured once per graph)
-                if (g->mean_weight == 0 && g->resident_edges > 0) {
-                    ws.bsum.ensure(kScanBlocks * 8);
-                    unsigned long long *acc = ws.bsum.as<unsigned long long>();
-                    PTG_CUDA_TRY(cudaMemsetAsync(acc, 0, 8, st));
-                    launch(ctx, "k_weight_sum", k_weight_sum, grid_for(g->resident_edges, kBlock, sms * 8), kBlock, 0,
-                           st, wt, g->resident_edges, acc);
-                    unsigned long long sum = 0;
-                    PTG_CUDA_TRY(cudaMemcpyAsync(&sum, acc, 8, cudaMemcpyDeviceToHost, st));
-                    PTG_CUDA_TRY(cudaStreamSynchronize(st));
-                    g->mean_weight = std::max(1.0, (double)sum / (double)g->resident_edges);
-                }
+                measure_mean_weight(g);
                 delta = (uint32_t)std::max(1.0, g->mean_weight > 0 ? g->mean_weight / 2 : 32.0);
             }
             init.threshold = base + delta;
@@ -543,11 +560,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
 
     bool allow_bu = kind == TRAV_BFS && g->symmetric && !g->out_of_core &&
                     !(flags & (PTG_NO_DIRECTION_OPT | PTG_REFERENCE_SCHEDULE));
-    if (allow_bu && !g->d_nzbm.p) {
-        g->d_nzbm.ensure(words * 4);
-        launch(ctx, "k_nonzero_bits", k_nonzero_bits<OffT>, grid_for(words, kBlock, sms * 8), kBlock, 0, st, off,
-               n, g->d_nzbm.as<uint32_t>());
-    }
+    if (allow_bu) build_nonzero_bits<OffT>(g);
     int cur = 0;
     uint64_t F = init.F, m_unvisited = g->m;
     bool far_nonempty = false;
@@ -722,6 +735,17 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
 }
 
 }  // namespace
+
+// Builds the per-graph tables the single-source traversals would otherwise
+// build on first use (bottom-up bitmap, SSSP bucket width).
+void trav_prepare_graph(ptg_graph *g) {
+    if (g->out_of_core) return;
+    if (g->symmetric) {
+        if (g->off64) build_nonzero_bits<unsigned long long>(g);
+        else build_nonzero_bits<uint32_t>(g);
+    }
+    measure_mean_weight(g);
+}
 
 void run_traversal(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value, uint32_t flags,
                    uint32_t delta, uint32_t max_iters, RunResult &rr) {

@@ -11,6 +11,7 @@ Reference mapping (ptGraph/main.cu:24-56):
   prCaculateIn{Share,Opt} (a stub there)    -> Graph.pagerank
 """
 import ctypes
+import weakref
 import os
 
 import numpy as np
@@ -97,15 +98,18 @@ class HostCsr(ctypes.Structure):
 
 
 class ServerConfig(ctypes.Structure):
-    _fields_ = [("max_slots", ctypes.c_uint32), ("max_batch", ctypes.c_uint32),
+    _fields_ = [("lanes", ctypes.c_uint32), ("max_slots", ctypes.c_uint32), ("max_batch", ctypes.c_uint32),
                 ("queue_capacity", ctypes.c_uint32), ("ppr_iterations", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("ppr_damping", ctypes.c_double),
                 ("memory_budget_bytes", ctypes.c_uint64)]
 
 
 class ServerStats(ctypes.Structure):
-    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64),
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
                 ("batches", ctypes.c_uint64), ("max_batch_seen", ctypes.c_uint64),
-                ("busy_ms", ctypes.c_double)]
+                ("budget_bytes", ctypes.c_uint64), ("committed_bytes", ctypes.c_uint64),
+                ("launches", ctypes.c_uint64), ("resident_graphs", ctypes.c_uint32),
+                ("streamed_graphs", ctypes.c_uint32), ("busy_ms", ctypes.c_double)]
 
 
 # Every function the header declares, with its ctypes signature.
@@ -133,6 +137,7 @@ _SIGS = {
     "ptg_cc": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(RunOpts)]),
     "ptg_pagerank": (ctypes.c_int, [_vp, _vp, ctypes.POINTER(PrOpts)]),
     "ptg_ppr": (ctypes.c_int, [_vp, ctypes.c_uint32, _vp, ctypes.POINTER(PrOpts)]),
+    "ptg_ppr_batch": (ctypes.c_int, [_vp, _u32p, ctypes.c_uint32, _vp, ctypes.POINTER(PrOpts)]),
     "ptg_bfs_noalloc": (ctypes.c_int, [_vp, _vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp,
                                        _vp]),
     "ptg_msbfs": (ctypes.c_int, [_vp, _u32p, ctypes.c_uint32, _vp, ctypes.POINTER(RunOpts)]),
@@ -142,6 +147,7 @@ _SIGS = {
     "ptg_server_create": (ctypes.c_int, [_vp, ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]),
     "ptg_server_destroy": (None, [_vp]),
     "ptg_server_add_graph": (ctypes.c_int, [_vp, _vp, _u32p]),
+    "ptg_server_upload": (ctypes.c_int, [_vp, ctypes.POINTER(Csr), _u32p, _u32p]),
     "ptg_server_submit": (ctypes.c_int, [_vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp,
                                          _u64p]),
     "ptg_server_wait": (ctypes.c_int, [_vp, ctypes.c_uint64, ctypes.c_int64,
@@ -222,10 +228,14 @@ class Ctx:
 
     def __init__(self, device=0):
         self.h = _vp()
+        self._deps = weakref.WeakSet()  # graphs and servers, closed before the context
         _check(lib().ptg_ctx_create(device, ctypes.byref(self.h)))
 
     def close(self):
         if self.h:
+            deps = list(self._deps)
+            for d in sorted(deps, key=lambda d: not isinstance(d, Server)):  # servers before graphs
+                d.close()
             lib().ptg_ctx_destroy(self.h)
             self.h = _vp()
 
@@ -315,6 +325,7 @@ class Graph:
         self.h = _vp()
         _check(lib().ptg_graph_create(ctx.h, ctypes.byref(c), ctypes.byref(config) if config else None,
                                       ctypes.byref(self.h)), ctx.h)
+        ctx._deps.add(self)
 
     def close(self):
         if self.h:
@@ -386,6 +397,19 @@ class Graph:
             stats.update(st.as_dict())
         return out
 
+    def ppr_batch(self, sources, iterations=20, damping=0.85, stats=None, out=None, flags=0):
+        s = np.ascontiguousarray(sources, dtype=np.uint32)
+        out = np.empty((s.size, self.n), dtype=np.float32) if out is None else out
+        o = PrOpts()
+        o.flags, o.iterations, o.damping = flags, iterations, damping
+        st = RunStats()
+        o.stats = ctypes.pointer(st)
+        _check(lib().ptg_ppr_batch(self.h, s.ctypes.data_as(_u32p), s.size, _ptr(out), ctypes.byref(o)),
+               self.ctx.h)
+        if stats is not None:
+            stats.update(st.as_dict())
+        return out
+
     def msbfs(self, sources, flags=0, stats=None):
         s = np.ascontiguousarray(sources, dtype=np.uint32)
         out = np.empty((s.size, self.n), dtype=np.uint32)
@@ -405,6 +429,95 @@ class Graph:
         if stats is not None:
             stats.update(st.as_dict())
         return out
+
+
+class Server:
+    """Request server (ptg_server_*): queries on registered graphs, served by
+    lanes that batch requests of the same graph and kind into fused passes."""
+
+    def __init__(self, ctx, lanes=0, max_slots=0, max_batch=0, queue_capacity=0, ppr_iterations=0,
+                 ppr_damping=0.0, memory_budget_bytes=0):
+        cfg = ServerConfig()
+        cfg.lanes, cfg.max_slots, cfg.max_batch = lanes, max_slots, max_batch
+        cfg.queue_capacity, cfg.ppr_iterations, cfg.ppr_damping = queue_capacity, ppr_iterations, ppr_damping
+        cfg.memory_budget_bytes = memory_budget_bytes
+        self.ctx = ctx
+        self.h = _vp()
+        _check(lib().ptg_server_create(ctx.h, ctypes.byref(cfg), ctypes.byref(self.h)), ctx.h)
+        ctx._deps.add(self)
+        self._keep = []      # graphs and uploaded arrays the server reads
+        self._n = {}         # graph id -> vertices
+        self._out = {}       # request id -> result buffer
+
+    def add_graph(self, graph):
+        gid = ctypes.c_uint32()
+        _check(lib().ptg_server_add_graph(self.h, graph.h, ctypes.byref(gid)), self.ctx.h)
+        self._keep.append(graph)
+        self._n[gid.value] = graph.n
+        return gid.value
+
+    def upload(self, offsets, col, weight=None, symmetric=True):
+        """Upload a sentinel-form CSR; returns (graph id, resident)."""
+        off = np.ascontiguousarray(offsets)
+        if off.dtype not in (np.uint32, np.uint64):
+            off = off.astype(np.uint64)
+        col = np.ascontiguousarray(col, dtype=np.uint32)
+        w = None if weight is None else np.ascontiguousarray(weight, dtype=np.uint32)
+        c = Csr()
+        c.n, c.m = off.size - 1, col.size
+        c.offsets = _ptr(off)
+        c.offset_type = PTG_OFFSETS_U64 if off.dtype == np.uint64 else PTG_OFFSETS_U32
+        c.offset_form = PTG_FORM_SENTINEL
+        if col.size == 0:
+            col = np.zeros(1, dtype=np.uint32)
+        c.col = _ptr(col)
+        c.weight = _ptr(w) if w is not None and c.m else None
+        c.flags = PTG_CSR_SYMMETRIC if symmetric else 0
+        gid = ctypes.c_uint32()
+        res = ctypes.c_uint32()
+        _check(lib().ptg_server_upload(self.h, ctypes.byref(c), ctypes.byref(gid), ctypes.byref(res)),
+               self.ctx.h)
+        self._keep.append((off, col, w))
+        self._n[gid.value] = off.size - 1
+        return gid.value, bool(res.value)
+
+    def submit(self, gid, kind, src, out=None):
+        """Queue a query; out (numpy array or CUDA tensor of n values) receives the result."""
+        if out is None:
+            out = np.empty(self._n.get(gid, 1), dtype=np.float32 if kind == PTG_Q_PPR else np.uint32)
+        rid = ctypes.c_uint64()
+        _check(lib().ptg_server_submit(self.h, gid, kind, src, _ptr(out), ctypes.byref(rid)), self.ctx.h)
+        self._out[rid.value] = out
+        return rid.value
+
+    def wait(self, rid, timeout_ms=-1):
+        """Wait for a request; returns (result, latency in microseconds)."""
+        lat = ctypes.c_double()
+        s = lib().ptg_server_wait(self.h, rid, timeout_ms, ctypes.byref(lat))
+        if s == PTG_ERR_TIMEOUT:
+            raise PtgError(s, "request not done in time")
+        out = self._out.pop(rid, None)
+        _check(s, self.ctx.h)
+        return out, lat.value
+
+    def drain(self):
+        _check(lib().ptg_server_drain(self.h), self.ctx.h)
+
+    def stats(self):
+        st = ServerStats()
+        _check(lib().ptg_server_stats_get(self.h, ctypes.byref(st)), self.ctx.h)
+        return {f: getattr(st, f) for f, _ in st._fields_}
+
+    def close(self):
+        if self.h:
+            lib().ptg_server_destroy(self.h)
+            self.h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def plan_partitions(offsets_n1, bytes_per_edge, device_free_bytes, config=None):

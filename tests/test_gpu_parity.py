@@ -238,3 +238,56 @@ def test_cc_batch_matches_per_graph(ptg, ctx, oracle):
         loff = (off[a:b + 1] - off[a]).astype(np.uint64)
         lcol = (col[e0:e1] - a).astype(np.uint32)
         assert (lab[a:b] == oracle.cc(loff, lcol, method="unionfind")).all()
+
+
+def _sym_csr(n, edges):
+    """Symmetric u64 CSR (sentinel form) from an undirected edge list, no duplicates."""
+    e = np.asarray(edges, dtype=np.int64).reshape(-1, 2)
+    e = e[e[:, 0] != e[:, 1]]
+    both = np.concatenate([e, e[:, ::-1]])
+    both = np.unique(both, axis=0)
+    off = np.zeros(n + 1, dtype=np.uint64)
+    np.add.at(off, both[:, 0] + 1, 1)
+    return np.cumsum(off).astype(np.uint64), both[:, 1].astype(np.uint32)
+
+
+@pytest.mark.parametrize("name", ["rmat10_sym", "rmat12_sym", "star20", "two_comp_isolated", "single_vertex",
+                                  "no_edges", "path10"])
+def test_ppr_batch_vs_oracle(ptg, ctx, oracle, name):
+    g = load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
+    n = g["off"].size - 1
+    G = ctx.graph(g["off"], g["col"], symmetric=True)
+    srcs = np.unique(np.concatenate([g["sources"], [0, n - 1]])).astype(np.uint32)
+    pb = G.ppr_batch(srcs)
+    for i, s in enumerate(srcs):
+        ref = oracle.ppr(g["off"], g["col"], int(s))
+        nz = ref > 1e-30
+        p = pb[i].astype(np.float64)
+        assert (p[~nz] < 1e-30).all()
+        assert (np.abs(p[nz] - ref[nz]) / ref[nz]).max() < PR_RTOL, (name, int(s))
+
+
+def test_ppr_batch_long_rows_and_independence(ptg, ctx, oracle):
+    """Rows longer than one warp's chunk (hubs of 5000 and 9000 edges), 40 sources
+    (two passes); a source's ranks are bit-identical alone and in any pass."""
+    rng = np.random.default_rng(21)
+    n = 12000
+    edges = [(0, v) for v in range(1, 5001)] + [(1, v) for v in range(3000, 12000)]
+    edges += list(map(tuple, rng.integers(0, n, (30000, 2))))
+    off, col = _sym_csr(n, edges)
+    G = ctx.graph(off, col, symmetric=True)
+    srcs = rng.choice(n, 40, replace=False).astype(np.uint32)
+    srcs[0], srcs[1] = 0, 1
+    pb = G.ppr_batch(srcs)
+    for i in list(range(0, 40, 6)) + [1]:
+        ref = oracle.ppr(off, col, int(srcs[i]))
+        nz = ref > 1e-30
+        p = pb[i].astype(np.float64)
+        assert (p[~nz] < 1e-30).all()
+        assert (np.abs(p[nz] - ref[nz]) / ref[nz]).max() < PR_RTOL
+        single = G.ppr(int(srcs[i])).astype(np.float64)
+        assert (np.abs(single[nz] - p[nz]) / ref[nz]).max() < 2 * PR_RTOL
+    alone = G.ppr_batch(srcs[5:6])
+    assert np.array_equal(alone[0].view(np.uint32), pb[5].view(np.uint32))
+    shuffled = G.ppr_batch(srcs[::-1].copy())
+    assert np.array_equal(shuffled[::-1].view(np.uint32), pb.view(np.uint32))
