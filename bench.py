@@ -241,7 +241,8 @@ def serve_workload(args):
            "resident_graph": pct(lat[big]), "uploaded_graphs": pct(lat[~big]),
            "server": {k: srv_stats[k] for k in ("batches", "max_batch_seen", "failed", "launches",
                                                  "resident_graphs", "streamed_graphs", "budget_bytes",
-                                                 "committed_bytes", "busy_ms")},
+                                                 "committed_bytes", "busy_ms", "fused_requests",
+                                                 "single_requests", "fused_batches", "fused_ms", "single_ms")},
            "lanes": args.serve_lanes, "graphs": {"resident_scale": args.serve_scale, "upload_scales": scales,
                                                  "admitted_resident": [bool(r) for _, r in up]},
            "gen_s": gen_s, "upload_s": upload_s}

@@ -340,6 +340,10 @@ typedef struct ptg_server_stats {
     uint64_t launches;        /* kernels launched by the lanes                    */
     uint32_t resident_graphs, streamed_graphs;
     double busy_ms;           /* summed lane time spent on batches                */
+    /* per kind (PTG_Q_*): requests served by fused passes / one at a time,
+     * fused passes run, and lane time spent on each */
+    uint64_t fused_requests[3], single_requests[3], fused_batches[3];
+    double fused_ms[3], single_ms[3];
 } ptg_server_stats;
 ptg_status ptg_server_stats_get(ptg_server *s, ptg_server_stats *st);
 

@@ -204,9 +204,19 @@ bool take_batch(ptg_server *s, Batch &b) {
     k = (uint32_t)std::min<uint64_t>(k, best->second.size());
     uint64_t left = s->budget > s->graph_bytes ? s->budget - s->graph_bytes : 0;
     uint64_t share = left / s->lanes.size();
-    while (k > 1 && batch_bytes(best->first.second, n, m, k) > share) k = (k + 1) / 2;
+    const uint32_t kd = best->first.second;
+    while (k > 1 && batch_bytes(kd, n, m, k) > share) k = (k + 1) / 2;
+    // one fused pass for k requests, or a single-source query: whichever the
+    // measured costs say is cheaper (a single query is measured first, then a
+    // pass).  A lane takes one request at a time when it runs singles, so the
+    // other lanes can serve the rest of the group concurrently.
+    if (e.g->out_of_core || k == 1) b.fused = false;
+    else if (e.single_ms[kd] < 0) b.fused = false;
+    else if (e.fused_ms[kd] < 0) b.fused = true;
+    else b.fused = e.fused_ms[kd] < k * e.single_ms[kd];
+    if (!b.fused) k = 1;
     b.graph = best->first.first;
-    b.kind = best->first.second;
+    b.kind = kd;
     for (uint32_t i = 0; i < k; i++) {
         uint64_t id = best->second.front();
         best->second.pop_front();
@@ -216,13 +226,6 @@ bool take_batch(ptg_server *s, Batch &b) {
         b.results.push_back(r.result);
     }
     if (e.g->out_of_core) e.busy = true;
-    // fused pass or single-source queries: whichever the measured costs say is
-    // cheaper for k requests (each is tried once first)
-    const uint32_t kd = b.kind;
-    if (e.g->out_of_core || k == 1) b.fused = false;
-    else if (e.single_ms[kd] < 0) b.fused = false;
-    else if (e.fused_ms[kd] < 0) b.fused = true;
-    else b.fused = e.fused_ms[kd] < k * e.single_ms[kd];
     s->queued -= k;
     s->inflight += k;
     return true;
@@ -312,7 +315,16 @@ void lane_loop(ptg_server *s, size_t li) {
             if (rs != PTG_OK) s->st.failed += b.ids.size();
             s->st.batches++;
             s->st.max_batch_seen = std::max<uint64_t>(s->st.max_batch_seen, b.ids.size());
-            s->st.busy_ms += std::chrono::duration<double, std::milli>(t1 - t0).count();
+            double bms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+            s->st.busy_ms += bms;
+            if (b.fused) {
+                s->st.fused_requests[b.kind] += b.ids.size();
+                s->st.fused_batches[b.kind]++;
+                s->st.fused_ms[b.kind] += bms;
+            } else {
+                s->st.single_requests[b.kind] += b.ids.size();
+                s->st.single_ms[b.kind] += bms;
+            }
         }
         s->cv_done.notify_all();
         s->cv_work.notify_all();  // slots and a streamed graph may have freed up

@@ -109,7 +109,10 @@ class ServerStats(ctypes.Structure):
                 ("batches", ctypes.c_uint64), ("max_batch_seen", ctypes.c_uint64),
                 ("budget_bytes", ctypes.c_uint64), ("committed_bytes", ctypes.c_uint64),
                 ("launches", ctypes.c_uint64), ("resident_graphs", ctypes.c_uint32),
-                ("streamed_graphs", ctypes.c_uint32), ("busy_ms", ctypes.c_double)]
+                ("streamed_graphs", ctypes.c_uint32), ("busy_ms", ctypes.c_double),
+                ("fused_requests", ctypes.c_uint64 * 3), ("single_requests", ctypes.c_uint64 * 3),
+                ("fused_batches", ctypes.c_uint64 * 3), ("fused_ms", ctypes.c_double * 3),
+                ("single_ms", ctypes.c_double * 3)]
 
 
 # Every function the header declares, with its ctypes signature.
@@ -506,7 +509,8 @@ class Server:
     def stats(self):
         st = ServerStats()
         _check(lib().ptg_server_stats_get(self.h, ctypes.byref(st)), self.ctx.h)
-        return {f: getattr(st, f) for f, _ in st._fields_}
+        return {f: (list(getattr(st, f)) if isinstance(getattr(st, f), ctypes.Array) else getattr(st, f))
+                for f, _ in st._fields_}
 
     def close(self):
         if self.h:
