@@ -33,6 +33,9 @@ sys.path.insert(0, os.path.join(ROOT, "test-world_gb300"))
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_spmv launch on
+# RMAT scale 22 (550.17 MB + 5.79 MB) / (n + m = 4,194,304 + 128,307,638)
+SPMV_DRAM_BYTES_PER_ITEM = (550.171648e6 + 5.786368e6) / (4194304 + 128307638)
 
 
 def parse():
@@ -575,15 +578,19 @@ def roofline(prof, n, m, step_edges, bfs_edges, args):
     top = max(prof.items(), key=lambda kv: kv[1][1])
     name, (cnt, tot) = top
     avg_ms = tot / max(cnt, 1)
+    traffic = None
     if name == "k_spmv":
         per_launch = 4 * (n + 1) + 8 * m + 8 * n  # one PageRank iteration
         unit_desc = "PageRank iteration: 4(n+1) + 8m + 8n bytes"
+        # DRAM bytes per launch from one ncu capture (profiles/k_spmv_rmat22.md):
+        # 556.0 MB over n + m = 132.5 M merge items, scaled by this graph's n + m
+        traffic = SPMV_DRAM_BYTES_PER_ITEM * (n + m)
     else:
         per_launch = None
         unit_desc = "no algorithmic byte model for %s yet" % name
     achieved = per_launch / (avg_ms / 1e3) / 1e9 if per_launch else None
     return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": hbm, "peak_kind": kind,
-            "unit": "GB/s", "frac": achieved / hbm if achieved else None, "traffic": None,
+            "unit": "GB/s", "frac": achieved / hbm if achieved else None, "traffic": traffic,
             "bytes_per_launch": per_launch, "avg_launch_ms": avg_ms, "launches": cnt, "model": unit_desc,
             "share_of_step": tot / sum(v[1] for v in prof.values())}
 
