@@ -272,6 +272,8 @@ void ptg_graph_destroy(ptg_graph *g) {
         if (g->stage_ready[i]) cudaEventDestroy(g->stage_ready[i]);
         if (g->stage_free[i]) cudaEventDestroy(g->stage_free[i]);
     }
+    for (int i = 0; i < 2; i++)
+        if (g->link_ev[i]) cudaEventDestroy(g->link_ev[i]);
     delete g;
 }
 
@@ -424,6 +426,7 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
                 if (g->weighted) g->stage_w[b].ensure(PE * 4);
                 PTG_CUDA_TRY(cudaEventCreateWithFlags(&g->stage_ready[b], cudaEventDisableTiming));
                 PTG_CUDA_TRY(cudaEventCreateWithFlags(&g->stage_free[b], cudaEventDisableTiming));
+                if (b < 2) PTG_CUDA_TRY(cudaEventCreate(&g->link_ev[b]));
             }
             g->device_bytes += (uint64_t)g->n_stage * PE * bpe;
             g->part_visits.assign(P, 0);

@@ -254,6 +254,7 @@ struct ptg_graph {
     uint32_t n_stage = 2;
     cudaEvent_t stage_ready[3] = {nullptr, nullptr, nullptr};
     cudaEvent_t stage_free[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t link_ev[2] = {nullptr, nullptr};  // first copy start / last copy end of a level
     uint64_t device_bytes = 0;
     // hot-partition residency
     uint32_t resident_policy = PTG_RESIDENT_PREFIX;

@@ -570,6 +570,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
     if (max_iters == 0) max_iters = (uint32_t)std::min<uint64_t>(0xFFFFFFF0ull, 4 * n + 16);
     const double alpha = 15.0, beta = 18.0;
 
+    bool link_open = false;  // a level's copies were recorded between link_ev[0] and link_ev[1]
     // out-of-core staging
     if (g->out_of_core) {
         ws.flags.ensure(g->num_partitions);
@@ -670,6 +671,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
                        g->resident_partitions, g->num_partitions, d_flags);
                 PTG_CUDA_TRY(cudaMemcpyAsync(h_flags, d_flags, g->num_partitions, cudaMemcpyDeviceToHost, st));
                 PTG_CUDA_TRY(cudaStreamSynchronize(st));
+                link_open = false;
                 for (uint64_t p = g->resident_partitions; p < g->num_partitions; p++) {
                     if (!h_flags[p]) {
                         rr.parts_skipped++;
@@ -681,6 +683,10 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
                     stage_next = (stage_next + 1) % (int)g->n_stage;
                     cudaStream_t cs = ctx->copy_stream;
                     PTG_CUDA_TRY(cudaStreamWaitEvent(cs, g->stage_free[b], 0));
+                    if (!link_open) {
+                        PTG_CUDA_TRY(cudaEventRecord(g->link_ev[0], cs));
+                        link_open = true;
+                    }
                     PTG_CUDA_TRY(cudaMemcpyAsync(g->stage_col[b].p, g->h_col + e0, (e1 - e0) * 4,
                                                  cudaMemcpyHostToDevice, cs));
                     rr.link_bytes += (e1 - e0) * 4;
@@ -710,6 +716,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
                     if (g->resident_policy == PTG_RESIDENT_HOT && p < g->part_visits.size())
                         g->part_visits[p]++;
                 }
+                if (link_open) PTG_CUDA_TRY(cudaEventRecord(g->link_ev[1], ctx->copy_stream));
             }
         }
         // next frontier: queue from the bitmap
@@ -718,6 +725,14 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
         PTG_CUDA_TRY(cudaStreamSynchronize(st));
         PTG_REQUIRE(h_ctl->error == 0, PTG_ERR_CUDA, "frontier overflow in relax");
+        if (link_open) {
+            // the level's copies, first start to last end (the compute stream
+            // waited on every one of them before the sync above)
+            float lms = 0.f;
+            PTG_CUDA_TRY(cudaEventElapsedTime(&lms, g->link_ev[0], g->link_ev[1]));
+            rr.link_ms += lms;
+            link_open = false;
+        }
         F = h_ctl->next_tail;
         if (use_far) far_nonempty = true;
         TravCtl upd = *h_ctl;

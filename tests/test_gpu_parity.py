@@ -163,7 +163,7 @@ def test_directed_rmat_out_of_core_vs_oracle(ptg, ctx, oracle):
     st = {}
     d = G.sssp(0, stats=st)
     assert (d == oracle.sssp(off, col, w, 0)).all()
-    assert st["partitions_streamed"] > 0 and st["link_bytes"] > 0
+    assert st["partitions_streamed"] > 0 and st["link_bytes"] > 0 and st["link_ms"] > 0
     assert (G.bfs(0) == oracle.bfs(off, col, 0, method="queue")).all()
     assert (G.cc() == oracle.cc(off, col)).all()
 
