@@ -13,13 +13,17 @@
 // fragment kernels 450-485.
 //
 // What changes on GB300:
-//  * The frontier is a compact queue plus a bitmap, built by the relax kernel
-//    itself (warp-aggregated appends, bitmap dedup), so no O(n) label scan is
-//    needed per round (reference: setLabeling + scan + compaction over n).
+//  * The next frontier is a bitmap: the relax kernel's improvements set bits
+//    with fire-and-forget atomic reductions (no return value awaited), and
+//    k_compact turns the bitmap into a queue in one pass over its words
+//    (n/8 bytes), so no O(n) label scan over 4-byte labels is needed per
+//    round (reference: setLabeling + Thrust scan + compaction over n).
 //  * Edges are expanded load-balanced: the frontier's degrees are scanned,
 //    and each 256-thread CTA takes a 2048-edge tile of the flattened edge
-//    space; consecutive threads read consecutive edges of one adjacency list
-//    (coalesced), a hub's edges spread over many CTAs (reference: one thread
+//    space (k_tile_rows precomputes each tile's first row).  A thread owns 8
+//    consecutive edge slots, walks the rows they cross in registers and keeps
+//    8 loads in flight; the column stream is read with an L2 evict-first
+//    policy.  A hub's edges spread over many CTAs (reference: one thread
 //    walks a whole adjacency list, gpu_kernels.cu:126).
 //  * BFS switches to bottom-up rounds (each unvisited vertex looks for a
 //    parent in the frontier bitmap) when the frontier's edges outweigh the
