@@ -33,9 +33,10 @@ sys.path.insert(0, os.path.join(ROOT, "test-world_gb300"))
 
 PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
-# ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_spmv launch on
-# RMAT scale 22 (550.17 MB + 5.79 MB) / (n + m = 4,194,304 + 128,307,638)
-SPMV_DRAM_BYTES_PER_ITEM = (550.171648e6 + 5.786368e6) / (4194304 + 128307638)
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of the SpMV kernels of one
+# PageRank iteration (k_pr_small/mid/big/chunks/long) on RMAT scale 22:
+# 670.73 MB + 5.08 MB over n + m = 4,194,304 + 128,307,638 items
+PR_DRAM_BYTES_PER_ITEM = (670.732288e6 + 5.081856e6) / (4194304 + 128307638)
 
 
 def parse():
@@ -645,24 +646,31 @@ def peaks():
 
 
 def roofline(prof, n, m, step_edges, bfs_edges, args):
-    """Roofline of the dominant kernel: algorithmic bytes per launch / its average launch time."""
+    """Roofline of the dominant kernel: algorithmic bytes per launch / its average launch time.
+    The PageRank SpMV kernels of one iteration (degree bins) count as one launch."""
     hbm, kind = peaks()
-    top = max(prof.items(), key=lambda kv: kv[1][1])
+    agg = dict(prof)
+    pr = [k for k in prof if k.startswith("k_pr_") and k != "k_pr_init" and not k.startswith("k_pr_bin")]
+    if pr and "k_pr_small" in prof:
+        for k in pr:
+            del agg[k]
+        agg["pagerank_spmv"] = (prof["k_pr_small"][0], sum(prof[k][1] for k in pr))
+    top = max(agg.items(), key=lambda kv: kv[1][1])
     name, (cnt, tot) = top
     avg_ms = tot / max(cnt, 1)
     traffic = None
-    if name == "k_spmv":
+    kernels = pr if name == "pagerank_spmv" else [name]
+    if name == "pagerank_spmv":
         per_launch = 4 * (n + 1) + 8 * m + 8 * n  # one PageRank iteration
-        unit_desc = "PageRank iteration: 4(n+1) + 8m + 8n bytes"
-        # DRAM bytes per launch from one ncu capture (profiles/k_spmv_rmat22.md):
-        # 556.0 MB over n + m = 132.5 M merge items, scaled by this graph's n + m
-        traffic = SPMV_DRAM_BYTES_PER_ITEM * (n + m)
+        unit_desc = "PageRank iteration (k_pr_small/mid/big/chunks/long): 4(n+1) + 8m + 8n bytes"
+        if PR_DRAM_BYTES_PER_ITEM:
+            traffic = PR_DRAM_BYTES_PER_ITEM * (n + m)
     else:
         per_launch = None
         unit_desc = "no algorithmic byte model for %s yet" % name
     achieved = per_launch / (avg_ms / 1e3) / 1e9 if per_launch else None
-    return {"kernel": name, "bound": "hbm", "achieved": achieved, "peak": hbm, "peak_kind": kind,
-            "unit": "GB/s", "frac": achieved / hbm if achieved else None, "traffic": traffic,
+    return {"kernel": name, "kernels": kernels, "bound": "hbm", "achieved": achieved, "peak": hbm,
+            "peak_kind": kind, "unit": "GB/s", "frac": achieved / hbm if achieved else None, "traffic": traffic,
             "bytes_per_launch": per_launch, "avg_launch_ms": avg_ms, "launches": cnt, "model": unit_desc,
             "share_of_step": tot / sum(v[1] for v in prof.values())}
 

@@ -23,6 +23,18 @@ using namespace ptg;
 
 namespace ptg {
 
+void stream_edges(ptg_graph *g, int which, void *dst, uint64_t e0, uint64_t e1, cudaStream_t cs) {
+    const uint32_t *base = which ? g->h_w : g->h_col;
+    uintptr_t s = (uintptr_t)(base + e0), t = (uintptr_t)(base + e1);
+    uintptr_t cut[4] = {s, std::min(std::max(g->pin_lo[which], s), t), std::min(std::max(g->pin_hi[which], s), t), t};
+    char *d = static_cast<char *>(dst);
+    for (int i = 0; i < 3; i++) {
+        if (cut[i + 1] <= cut[i]) continue;
+        PTG_CUDA_TRY(cudaMemcpyAsync(d + (cut[i] - s), (const void *)cut[i], cut[i + 1] - cut[i],
+                                     cudaMemcpyHostToDevice, cs));
+    }
+}
+
 void set_error(ptg_ctx *ctx, const Error &e) {
     if (ctx) ctx->last_error = e.msg;
 }
@@ -404,12 +416,19 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
             } else {
                 // register the caller's streamed range (page-aligned)
                 size_t pg = host_page();
-                auto reg = [&](const uint32_t *base, PinnedBuf &fallback, const uint32_t *&dst) {
+                auto reg = [&](const uint32_t *base, PinnedBuf &fallback, const uint32_t *&dst, int which) {
+                    // only whole pages inside the caller's array: pages it shares
+                    // with other allocations may be unmapped and reused by the
+                    // process while still registered.  Copies that touch the
+                    // unregistered head and tail go through the pageable path.
                     uintptr_t a = (uintptr_t)(base + e0), b = (uintptr_t)(base + g->m);
-                    uintptr_t a0 = a & ~(uintptr_t)(pg - 1), b1 = (b + pg - 1) & ~(uintptr_t)(pg - 1);
-                    cudaError_t e = cudaHostRegister((void *)a0, b1 - a0, cudaHostRegisterDefault);
+                    uintptr_t a0 = (a + pg - 1) & ~(uintptr_t)(pg - 1), b1 = b & ~(uintptr_t)(pg - 1);
+                    cudaError_t e = b1 > a0 ? cudaHostRegister((void *)a0, b1 - a0, cudaHostRegisterDefault)
+                                            : cudaErrorInvalidValue;
                     if (e == cudaSuccess) {
                         g->registered.push_back((void *)a0);
+                        g->pin_lo[which] = a0;
+                        g->pin_hi[which] = b1;
                         dst = base;
                     } else {
                         cudaGetLastError();
@@ -418,8 +437,8 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
                         dst = fallback.as<uint32_t>();
                     }
                 };
-                reg(hc, g->own_col, g->h_col);
-                if (hw) reg(hw, g->own_w, g->h_w);
+                reg(hc, g->own_col, g->h_col, 0);
+                if (hw) reg(hw, g->own_w, g->h_w, 1);
             }
             for (uint32_t b = 0; b < g->n_stage; b++) {
                 g->stage_col[b].ensure(PE * 4);

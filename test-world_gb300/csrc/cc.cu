@@ -131,8 +131,7 @@ void cc_hook_impl(ptg_graph *g, uint32_t *d_label, RunResult &rr) {
             uint64_t e0 = p * g->partition_edges, e1 = std::min<uint64_t>(g->m, e0 + g->partition_edges);
             cudaStream_t cs = ctx->copy_stream;
             PTG_CUDA_TRY(cudaStreamWaitEvent(cs, g->stage_free[b], 0));
-            PTG_CUDA_TRY(cudaMemcpyAsync(g->stage_col[b].p, g->h_col + e0, (e1 - e0) * 4,
-                                         cudaMemcpyHostToDevice, cs));
+            stream_edges(g, 0, g->stage_col[b].p, e0, e1, cs);
             PTG_CUDA_TRY(cudaEventRecord(g->stage_ready[b], cs));
             PTG_CUDA_TRY(cudaStreamWaitEvent(st, g->stage_ready[b], 0));
             launch(ctx, "k_hook_partition", k_hook<OffT>, grid_for(e1 - e0, kTile, sms * 16), kBlock, 0, st,

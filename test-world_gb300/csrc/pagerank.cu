@@ -11,26 +11,18 @@
 // are compensated two-float sums (about 48 significant bits, beyond what the
 // 1e-6 tolerance needs), because GB300 runs FP32 adds at 64x its FP64 rate.
 //
-// Pull over a symmetric CSR (in-edges == out-edges).  Each iteration is one
-// merge-path SpMV (Merrill & Garland): the n row ends and m edges form n+m
-// merge items cut into 1792-item tiles, one CTA per tile, 7 items per thread,
-// so a hub's row spreads over as many threads and CTAs as it needs.  The
-// tile boundaries depend only on the graph and are computed once
-// (merge_tiles).  A CTA stages its row ends and the gathered contributions
-// contrib[col[j]] of its edges in shared memory with coalesced loads, each
-// thread merges its items sequentially, and a segmented warp scan combines
-// the partial sums of rows that span threads.  Rows that start and end in
-// the CTA are finalized in place; a row crossing a CTA boundary adds its
-// pieces to an FP64 accumulator (about two global atomics per tile) and is
-// finalized by one fixup thread.
+// Pull over a symmetric CSR (in-edges == out-edges), as a degree-binned
+// SpMV: rows are grouped once per graph by degree (a thread, 8 lanes or a
+// warp per row, and warp-sized chunks of the longest rows), each lane keeps
+// its own two-float partial, and partials meet through shuffles in a fixed
+// order, so the result of a row does not depend on scheduling.  The gathered
+// contributions of a scale-24 graph (67 MB) stay in L2; DRAM carries the
+// column stream, so the gathers' L2 sector traffic is the bound.
 #include <algorithm>
 
 #include "ptg_device.cuh"
 
 namespace ptg {
-
-constexpr int kPrItems = 7;
-constexpr int kPrTile = kBlock * kPrItems;
 
 namespace {
 
@@ -63,43 +55,15 @@ struct PrArgs {
     uint64_t n, m;
     const void *off;          // OffT[n+1]
     const uint32_t *col;
-    const uint64_t *tiles;    // row index at each tile's first merge item
     const float *contrib_in;  // [n]
     float *contrib_out;       // [n]
     float *rank_out;          // [n] or nullptr (written on the last iteration)
-    double *acc;              // [n] zero on entry; split rows only, re-zeroed by fixup
-    uint32_t *split_rows;     // rows that cross a CTA boundary (listed by their first CTA)
-    unsigned *split_count;
-    uint32_t split_cap;
     const double *dangling_in;
     double *dangling_out;
     double d;
     int personalized;
     uint32_t src;
 };
-
-// Number of row ends among the first `diag` merge items (Merrill's merge-path
-// search): row end i is taken before edge j when off[i+1] <= j.
-template <class OffT>
-__device__ __forceinline__ uint64_t merge_search(const OffT *row_end, uint64_t n, uint64_t m,
-                                                 uint64_t diag) {
-    uint64_t lo = diag > m ? diag - m : 0, hi = min(diag, n);
-    while (lo < hi) {
-        uint64_t mid = (lo + hi) >> 1;
-        if ((uint64_t)row_end[mid] <= diag - mid - 1) lo = mid + 1;
-        else hi = mid;
-    }
-    return lo;
-}
-
-template <class OffT>
-__global__ void k_merge_tiles(const OffT *off, uint64_t n, uint64_t m, uint64_t ntiles, uint64_t *tiles) {
-    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t <= ntiles;
-         t += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t d = min(t * (uint64_t)kPrTile, n + m);
-        tiles[t] = merge_search(off + 1, n, m, d);
-    }
-}
 
 // Two-float product (fma gives the exact rounding error of hi*hi).
 __device__ __forceinline__ ff ff_mul(ff a, ff b) {
@@ -148,157 +112,6 @@ __device__ __forceinline__ void finalize_row(const PrArgs &a, const PrConst &c, 
     }
 }
 
-template <class OffT>
-__global__ void __launch_bounds__(kBlock, 8) k_spmv(PrArgs a) {
-    __shared__ OffT s_end[kPrTile + 1];   // row ends of the CTA's rows
-    __shared__ float s_val[kPrTile + 1];  // gathered contributions of its edges
-    __shared__ uint32_t s_key[kBlock];    // carry row per thread (local index)
-    __shared__ float s_shi[kBlock], s_slo[kBlock];
-    __shared__ uint32_t s_wfirst[kBlock / 32], s_wlast[kBlock / 32];
-    __shared__ float s_whi[kBlock / 32], s_wlo[kBlock / 32];
-    const OffT *off = reinterpret_cast<const OffT *>(a.off);
-    const OffT *row_end = off + 1;
-    const uint64_t n = a.n, m = a.m, total = n + m;
-    const PrConst c = pr_const(a);
-    const uint32_t NONE = 0xFFFFFFFFu;
-    ff dang_local{0.f, 0.f};
-    uint64_t ntiles = (total + kPrTile - 1) / kPrTile;
-    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        uint64_t d0 = tile * kPrTile, d1 = min(total, d0 + kPrTile);
-        uint64_t i0 = a.tiles[tile], i1 = a.tiles[tile + 1];
-        uint64_t j0 = d0 - i0, j1 = d1 - i1;
-        // tile-local counts and positions fit 32 bits (at most kPrTile items)
-        uint32_t nrows = (uint32_t)(i1 - i0), nedges = (uint32_t)(j1 - j0);
-        for (uint32_t k = threadIdx.x; k <= nrows; k += kBlock)
-            s_end[k] = (i0 + k < n) ? row_end[i0 + k] : (OffT)m;
-        for (uint32_t k = threadIdx.x; k < nedges; k += kBlock) s_val[k] = a.contrib_in[__ldcs(a.col + j0 + k)];
-        __syncthreads();
-        // this thread's merge items inside the tile; edge positions are local
-        // (edge j0 + x is x), row ends are converted on the fly
-        uint32_t items = nrows + nedges;
-        uint32_t td0 = min((uint32_t)threadIdx.x * kPrItems, items);
-        uint32_t td1 = min(td0 + kPrItems, items);
-        uint32_t lo = td0 > nedges ? td0 - nedges : 0, hi = min(td0, nrows);
-        while (lo < hi) {
-            uint32_t mid = (lo + hi) >> 1;
-            if ((uint32_t)(s_end[mid] - (OffT)j0) <= td0 - mid - 1) lo = mid + 1;
-            else hi = mid;
-        }
-        uint32_t li = lo, lj = td0 - lo;
-        // local start of the row the thread starts in (may be before the tile)
-        int64_t row_start = (li == 0) ? (int64_t)off[i0] - (int64_t)j0 : (int64_t)(s_end[li - 1] - (OffT)j0);
-        bool cont = (int64_t)lj > row_start;  // first row is a continuation
-        uint32_t first_row = NONE;
-        ff first_val{0.f, 0.f};
-        ff sum{0.f, 0.f};
-        uint32_t end_l = li < nrows ? (uint32_t)(s_end[li] - (OffT)j0) : 0xFFFFFFFFu;
-        for (uint32_t k = td0; k < td1; k++) {
-            if (lj >= end_l) {
-                if (cont) {  // combined with earlier threads after the scan
-                    first_row = li;
-                    first_val = sum;
-                    cont = false;
-                } else {
-                    finalize_row<OffT>(a, c, i0 + li, (OffT)(end_l - row_start), sum, dang_local);
-                }
-                row_start = end_l;
-                sum = ff{0.f, 0.f};
-                li++;
-                end_l = li < nrows ? (uint32_t)(s_end[li] - (OffT)j0) : 0xFFFFFFFFu;
-            } else {
-                sum = ff_add(sum, s_val[lj]);
-                lj++;
-            }
-        }
-        // carry: the row in progress at the end of this thread's items
-        uint32_t key = (li < nrows || (i0 + li < n && (int64_t)lj > row_start)) ? li : NONE;
-        if (td0 >= td1) key = NONE;
-        // segmented inclusive scan of carries by row (warp level)
-        unsigned lane = lane_id(), wid = threadIdx.x >> 5;
-        ff s = key == NONE ? ff{0.f, 0.f} : sum;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t ok = __shfl_up_sync(0xffffffffu, key, o);
-            float oh = __shfl_up_sync(0xffffffffu, s.hi, o);
-            float ol = __shfl_up_sync(0xffffffffu, s.lo, o);
-            if (lane >= (unsigned)o && ok == key && key != NONE) s = ff_add(s, ff{oh, ol});
-        }
-        uint32_t wfirst = __shfl_sync(0xffffffffu, key, 0);
-        if (lane == 31) {
-            s_wlast[wid] = key;
-            s_whi[wid] = s.hi;
-            s_wlo[wid] = s.lo;
-        }
-        if (lane == 0) s_wfirst[wid] = wfirst;
-        __syncthreads();
-        // carries from earlier warps continuing the same row
-        if (key != NONE && key == wfirst) {
-            for (int w = (int)wid - 1; w >= 0; w--) {
-                if (s_wlast[w] != key) break;
-                s = ff_add(s, ff{s_whi[w], s_wlo[w]});
-                if (s_wfirst[w] != key) break;
-            }
-        }
-        s_key[threadIdx.x] = key;
-        s_shi[threadIdx.x] = s.hi;
-        s_slo[threadIdx.x] = s.lo;
-        __syncthreads();
-        // the first row this thread ended: add the carries of earlier threads
-        if (first_row != NONE) {
-            ff tot = first_val;
-            if (threadIdx.x > 0 && s_key[threadIdx.x - 1] == first_row)
-                tot = ff_add(tot, ff{s_shi[threadIdx.x - 1], s_slo[threadIdx.x - 1]});
-            uint64_t v = i0 + first_row;
-            uint64_t rs = first_row == 0 ? (uint64_t)off[i0] : (uint64_t)s_end[first_row - 1];
-            if (rs < j0) {
-                atomicAdd(&a.acc[v], ff_dbl(tot));  // began in an earlier CTA: fixup finalizes
-            } else {
-                OffT deg = s_end[first_row] - (OffT)rs;
-                finalize_row<OffT>(a, c, v, deg, tot, dang_local);
-            }
-        }
-        // Row i1 (local index nrows) is the only row that can still be open at
-        // the end of the tile; if it has edges here it continues in a later
-        // CTA.  Its carry is the scan value of the last thread keyed to it.
-        if (threadIdx.x == kBlock - 1 && i1 < n) {
-            uint64_t rs = nrows == 0 ? (uint64_t)off[i0] : (uint64_t)s_end[nrows - 1];
-            if (j1 > rs) {
-                ff tot{0.f, 0.f};
-                for (int t = kBlock - 1; t >= 0; t--) {
-                    if (s_key[t] == (uint32_t)nrows) {
-                        tot = ff{s_shi[t], s_slo[t]};
-                        break;
-                    }
-                }
-                atomicAdd(&a.acc[i1], ff_dbl(tot));
-                if (rs >= j0) {  // it began in this tile: list it once for the fixup
-                    unsigned pos = atomicAdd(a.split_count, 1u);
-                    if (pos < a.split_cap) a.split_rows[pos] = (uint32_t)i1;
-                }
-            }
-        }
-        __syncthreads();
-    }
-    double sd = block_reduce_sum(ff_dbl(dang_local));
-    if (threadIdx.x == 0 && sd != 0.0) atomicAdd(a.dangling_out, sd);
-}
-
-// Finalize rows that crossed a CTA boundary (each listed once; split rows
-// have edges, so none of them adds dangling mass).
-template <class OffT>
-__global__ void __launch_bounds__(kBlock) k_fixup(PrArgs a) {
-    const OffT *off = reinterpret_cast<const OffT *>(a.off);
-    unsigned cnt = min(*a.split_count, a.split_cap);
-    const PrConst c = pr_const(a);
-    ff dl{0.f, 0.f};
-    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < cnt; i += gridDim.x * blockDim.x) {
-        uint32_t v = a.split_rows[i];
-        double s = a.acc[v];
-        a.acc[v] = 0.0;
-        finalize_row<OffT>(a, c, v, off[v + 1] - off[v], ff_of(s), dl);
-    }
-}
-
 // contrib0 = r0 / deg, dangling0 = sum of r0 over zero-degree vertices.
 template <class OffT>
 __global__ void __launch_bounds__(kBlock) k_pr_init(const OffT *off, uint64_t n, int personalized,
@@ -319,6 +132,264 @@ __global__ void __launch_bounds__(kBlock) k_pr_init(const OffT *off, uint64_t n,
     if (threadIdx.x == 0 && s != 0.0) atomicAdd(dangling, s);
 }
 
+// ---------------------------------------------------------------------------
+// Degree-binned SpMV.  Rows are split once per graph by degree:
+//   deg <= kPrSmall          one thread per row (k_pr_small walks all rows)
+//   kPrSmall < deg <= kPrMid 8 lanes per row (list `mid`)
+//   kPrMid < deg <= kPrChunk one warp per row (list `big`)
+//   deg > kPrChunk           kPrChunk-edge chunks, one warp each, whose
+//                            partial sums are added in chunk order (k_pr_long)
+// Every lane keeps its own two-float partial (independent dependency chains),
+// partials meet through shuffles in a fixed order, so a row's sum depends
+// only on the row.  No shared-memory staging and no CTA barriers; the lists
+// hold rows in ascending order, so rank and contribution stores of
+// neighbouring lanes fall in the same lines.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kPrSmall = 4;
+constexpr uint32_t kPrMid = 64;
+constexpr uint32_t kPrChunk = 4096;
+
+struct PrBins {
+    const uint32_t *mid;
+    uint64_t n_mid;
+    const uint32_t *big;
+    uint64_t n_big;
+    const uint2 *items;  // (row, chunk)
+    uint64_t n_items;
+    const uint2 *longs;  // (row, first item)
+    uint64_t n_longs;
+    float2 *partial;     // [n_items]
+};
+
+__device__ __forceinline__ ff ff_shfl_xor(ff s, int o, int width) {
+    return ff{__shfl_xor_sync(0xffffffffu, s.hi, o, width), __shfl_xor_sync(0xffffffffu, s.lo, o, width)};
+}
+
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_pr_small(PrArgs a) {
+    const OffT *off = reinterpret_cast<const OffT *>(a.off);
+    const PrConst c = pr_const(a);
+    ff dl{0.f, 0.f};
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < a.n; v += (uint64_t)gridDim.x * blockDim.x) {
+        OffT b = off[v], e = off[v + 1];
+        OffT deg = e - b;
+        if ((uint64_t)deg > kPrSmall) continue;
+        float x[kPrSmall];
+#pragma unroll
+        for (uint32_t t = 0; t < kPrSmall; t++) x[t] = t < (uint32_t)deg ? a.contrib_in[__ldcs(a.col + b + t)] : 0.f;
+        ff s{0.f, 0.f};
+#pragma unroll
+        for (uint32_t t = 0; t < kPrSmall; t++)
+            if (t < (uint32_t)deg) s = ff_add(s, x[t]);
+        finalize_row<OffT>(a, c, v, deg, s, dl);
+    }
+    double sd = block_reduce_sum(ff_dbl(dl));
+    if (threadIdx.x == 0 && sd != 0.0) atomicAdd(a.dangling_out, sd);
+}
+
+// 8 lanes per row: lane j sums edges j, j+8, ... (two gathers in flight).
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_pr_mid(PrArgs a, PrBins bins) {
+    const OffT *off = reinterpret_cast<const OffT *>(a.off);
+    const PrConst c = pr_const(a);
+    const unsigned sub = threadIdx.x & 7u;
+    ff dl{0.f, 0.f};
+    const uint64_t groups = (uint64_t)gridDim.x * blockDim.x / 8;
+    const uint64_t span = (bins.n_mid + 3) / 4 * 4;  // whole warps stay in the loop for the shuffles
+    for (uint64_t gi = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 8; gi < span; gi += groups) {
+        bool valid = gi < bins.n_mid;
+        uint32_t v = valid ? bins.mid[gi] : 0u;
+        OffT b = valid ? off[v] : (OffT)0, e = valid ? off[v + 1] : (OffT)0;
+        ff s{0.f, 0.f};
+        OffT k = b + sub;
+        for (; k + 8 < e; k += 16) {
+            float x0 = a.contrib_in[__ldcs(a.col + k)];
+            float x1 = a.contrib_in[__ldcs(a.col + k + 8)];
+            s = ff_add(s, x0);
+            s = ff_add(s, x1);
+        }
+        if (k < e) s = ff_add(s, a.contrib_in[__ldcs(a.col + k)]);
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) s = ff_add(s, ff_shfl_xor(s, o, 8));
+        if (valid && sub == 0) finalize_row<OffT>(a, c, v, e - b, s, dl);
+    }
+}
+
+// One warp per row: lane j sums edges j, j+32, ... (four gathers in flight).
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_pr_big(PrArgs a, PrBins bins) {
+    const OffT *off = reinterpret_cast<const OffT *>(a.off);
+    const PrConst c = pr_const(a);
+    const unsigned lane = lane_id();
+    ff dl{0.f, 0.f};
+    const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
+    for (uint64_t wi = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; wi < bins.n_big; wi += warps) {
+        uint32_t v = bins.big[wi];
+        OffT b = off[v], e = off[v + 1];
+        ff s{0.f, 0.f};
+        OffT k = b + lane;
+        for (; k + 96 < e; k += 128) {
+            float x0 = a.contrib_in[__ldcs(a.col + k)];
+            float x1 = a.contrib_in[__ldcs(a.col + k + 32)];
+            float x2 = a.contrib_in[__ldcs(a.col + k + 64)];
+            float x3 = a.contrib_in[__ldcs(a.col + k + 96)];
+            s = ff_add(s, x0);
+            s = ff_add(s, x1);
+            s = ff_add(s, x2);
+            s = ff_add(s, x3);
+        }
+        for (; k < e; k += 32) s = ff_add(s, a.contrib_in[__ldcs(a.col + k)]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s = ff_add(s, ff_shfl_xor(s, o, 32));
+        if (lane == 0) finalize_row<OffT>(a, c, v, e - b, s, dl);
+    }
+}
+
+// Chunks of rows longer than kPrChunk: one warp per chunk, partial sums out.
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_pr_chunks(PrArgs a, PrBins bins) {
+    const OffT *off = reinterpret_cast<const OffT *>(a.off);
+    const unsigned lane = lane_id();
+    const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
+    for (uint64_t it = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; it < bins.n_items; it += warps) {
+        uint2 item = bins.items[it];
+        OffT b = off[item.x] + (OffT)item.y * (OffT)kPrChunk;
+        OffT e = off[(uint64_t)item.x + 1];
+        if (e - b > (OffT)kPrChunk) e = b + (OffT)kPrChunk;
+        ff s{0.f, 0.f};
+        OffT k = b + lane;
+        for (; k + 96 < e; k += 128) {
+            float x0 = a.contrib_in[__ldcs(a.col + k)];
+            float x1 = a.contrib_in[__ldcs(a.col + k + 32)];
+            float x2 = a.contrib_in[__ldcs(a.col + k + 64)];
+            float x3 = a.contrib_in[__ldcs(a.col + k + 96)];
+            s = ff_add(s, x0);
+            s = ff_add(s, x1);
+            s = ff_add(s, x2);
+            s = ff_add(s, x3);
+        }
+        for (; k < e; k += 32) s = ff_add(s, a.contrib_in[__ldcs(a.col + k)]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s = ff_add(s, ff_shfl_xor(s, o, 32));
+        if (lane == 0) bins.partial[it] = make_float2(s.hi, s.lo);
+    }
+}
+
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_pr_long(PrArgs a, PrBins bins) {
+    const OffT *off = reinterpret_cast<const OffT *>(a.off);
+    const PrConst c = pr_const(a);
+    ff dl{0.f, 0.f};
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < bins.n_longs;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        uint2 L = bins.longs[j];
+        OffT deg = off[(uint64_t)L.x + 1] - off[L.x];
+        uint32_t pieces = (uint32_t)(((uint64_t)deg + kPrChunk - 1) / kPrChunk);
+        ff s{0.f, 0.f};
+        for (uint32_t i = 0; i < pieces; i++) {
+            float2 p = bins.partial[(uint64_t)L.y + i];
+            s = ff_add(s, ff{p.x, p.y});
+        }
+        finalize_row<OffT>(a, c, L.x, deg, s, dl);
+    }
+}
+
+// Bin construction, in two passes over contiguous vertex ranges (one per
+// CTA) so that each list keeps ascending row order.  counts[blk*4 + t]:
+// rows of `mid`, rows of `big`, rows of `longs`, chunk items.
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_pr_bin_count(const OffT *off, uint64_t n, unsigned long long *counts) {
+    uint64_t per = (n + gridDim.x - 1) / gridDim.x;
+    uint64_t v0 = blockIdx.x * per, v1 = min(n, v0 + per);
+    unsigned long long cm = 0, cb = 0, cl = 0, ci = 0;
+    for (uint64_t v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
+        uint64_t deg = (uint64_t)(off[v + 1] - off[v]);
+        if (deg <= kPrSmall) continue;
+        if (deg <= kPrMid) cm++;
+        else if (deg <= kPrChunk) cb++;
+        else {
+            cl++;
+            ci += (deg + kPrChunk - 1) / kPrChunk;
+        }
+    }
+    cm = block_reduce_sum(cm);
+    cb = block_reduce_sum(cb);
+    cl = block_reduce_sum(cl);
+    ci = block_reduce_sum(ci);
+    if (threadIdx.x == 0) {
+        counts[blockIdx.x * 4 + 0] = cm;
+        counts[blockIdx.x * 4 + 1] = cb;
+        counts[blockIdx.x * 4 + 2] = cl;
+        counts[blockIdx.x * 4 + 3] = ci;
+    }
+}
+
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_pr_bin_fill(const OffT *off, uint64_t n, const unsigned long long *base,
+                                                        uint32_t *mid, uint32_t *big, uint2 *longs, uint2 *items) {
+    uint64_t per = (n + gridDim.x - 1) / gridDim.x;
+    uint64_t v0 = blockIdx.x * per, v1 = min(n, v0 + per);
+    unsigned long long bm = base[blockIdx.x * 4 + 0], bb = base[blockIdx.x * 4 + 1];
+    unsigned long long bl = base[blockIdx.x * 4 + 2], bi = base[blockIdx.x * 4 + 3];
+    for (uint64_t c0 = v0; c0 < v1; c0 += blockDim.x) {
+        uint64_t v = c0 + threadIdx.x;
+        uint64_t deg = v < v1 ? (uint64_t)(off[v + 1] - off[v]) : 0;
+        unsigned long long fm = deg > kPrSmall && deg <= kPrMid, fb = deg > kPrMid && deg <= kPrChunk;
+        unsigned long long fl = deg > kPrChunk, fi = fl ? (deg + kPrChunk - 1) / kPrChunk : 0;
+        unsigned long long tm, tb, tl, ti;
+        unsigned long long pm = block_exclusive_scan(fm, tm);
+        unsigned long long pb = block_exclusive_scan(fb, tb);
+        unsigned long long pl = block_exclusive_scan(fl, tl);
+        unsigned long long pi = block_exclusive_scan(fi, ti);
+        if (fm) mid[bm + pm] = (uint32_t)v;
+        if (fb) big[bb + pb] = (uint32_t)v;
+        if (fl) {
+            longs[bl + pl] = make_uint2((uint32_t)v, (uint32_t)(bi + pi));
+            for (unsigned long long i = 0; i < fi; i++) items[bi + pi + i] = make_uint2((uint32_t)v, (uint32_t)i);
+        }
+        bm += tm;
+        bb += tb;
+        bl += tl;
+        bi += ti;
+    }
+}
+
+template <class OffT>
+void build_pr_bins(ptg_graph *g) {
+    ptg_ctx *ctx = g->ctx;
+    cudaStream_t st = ctx->stream;
+    const OffT *off = g->d_off.as<OffT>();
+    const int nb = (int)std::min<uint64_t>(1024, std::max<uint64_t>(1, (g->n + kBlock - 1) / kBlock));
+    DevBuf counts;
+    counts.ensure((uint64_t)nb * 4 * 8);
+    launch(ctx, "k_pr_bin_count", k_pr_bin_count<OffT>, nb, kBlock, 0, st, off, g->n,
+           counts.as<unsigned long long>());
+    std::vector<unsigned long long> h((size_t)nb * 4);
+    PTG_CUDA_TRY(cudaMemcpyAsync(h.data(), counts.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
+    PTG_CUDA_TRY(cudaStreamSynchronize(st));
+    unsigned long long tot[4] = {0, 0, 0, 0};
+    for (int b = 0; b < nb; b++)
+        for (int t = 0; t < 4; t++) {
+            unsigned long long x = h[(size_t)b * 4 + t];
+            h[(size_t)b * 4 + t] = tot[t];
+            tot[t] += x;
+        }
+    PTG_CUDA_TRY(cudaMemcpyAsync(counts.p, h.data(), h.size() * 8, cudaMemcpyHostToDevice, st));
+    g->d_pr_mid.ensure(std::max<unsigned long long>(tot[0], 1) * 4);
+    g->d_pr_big.ensure(std::max<unsigned long long>(tot[1], 1) * 4);
+    g->d_pr_longs.ensure(std::max<unsigned long long>(tot[2], 1) * 8);
+    g->d_pr_items.ensure(std::max<unsigned long long>(tot[3], 1) * 8);
+    launch(ctx, "k_pr_bin_fill", k_pr_bin_fill<OffT>, nb, kBlock, 0, st, off, g->n,
+           (const unsigned long long *)counts.p, g->d_pr_mid.as<uint32_t>(), g->d_pr_big.as<uint32_t>(),
+           g->d_pr_longs.as<uint2>(), g->d_pr_items.as<uint2>());
+    PTG_CUDA_TRY(cudaStreamSynchronize(st));
+    g->n_pr_mid = tot[0];
+    g->n_pr_big = tot[1];
+    g->n_pr_longs = tot[2];
+    g->n_pr_items = tot[3];
+    g->pr_bins_built = true;
+}
+
 template <class OffT>
 void pagerank_impl(ptg_graph *g, bool personalized, uint32_t src, double damping, uint32_t iters,
                    float *d_rank, RunResult &rr) {
@@ -327,76 +398,70 @@ void pagerank_impl(ptg_graph *g, bool personalized, uint32_t src, double damping
     cudaStream_t st = ctx->stream;
     const uint64_t n = g->n, m = g->m;
     const int sms = ctx->sm_count;
-    uint64_t ntiles = (n + m + kPrTile - 1) / kPrTile;
-    const uint64_t *tiles = merge_tiles(g);
-    uint32_t split_cap = (uint32_t)std::min<uint64_t>(ntiles + 1, 0xFFFFFFF0ull);
-    ws.aux.ensure(n * 8 + 64);       // acc
-    ws.aux2.ensure(2 * n * 4 + 64);  // contrib ping-pong
-    ws.q[0].ensure(std::max<uint64_t>((uint64_t)split_cap * 4, n * 4));
+    if (!g->pr_bins_built) build_pr_bins<OffT>(g);
+    ws.aux.ensure(std::max<uint64_t>(g->n_pr_items, 1) * 8);  // chunk partials
+    ws.aux2.ensure(2 * n * 4 + 64);                          // contrib ping-pong
     ws.bsum.ensure(1024 * 8);
-    double *acc = ws.aux.as<double>();
     float *contrib[2] = {ws.aux2.as<float>(), ws.aux2.as<float>() + n};
     double *dang = ws.bsum.as<double>();  // dang[0], dang[1]
-    unsigned *split_count = reinterpret_cast<unsigned *>(ws.bsum.as<double>() + 4);
-    PTG_CUDA_TRY(cudaMemsetAsync(acc, 0, n * 8, st));
     PTG_CUDA_TRY(cudaMemsetAsync(dang, 0, 64, st));
     int fill_grid = grid_for(n, kBlock, sms * 8);
     const OffT *off = g->d_off.as<OffT>();
     launch(ctx, "k_pr_init", k_pr_init<OffT>, fill_grid, kBlock, 0, st, off, n, personalized ? 1 : 0, src,
            contrib[0], &dang[0]);
-    int grid = grid_for(ntiles, 1, sms * 8);
+    PrBins bins;
+    bins.mid = g->d_pr_mid.as<uint32_t>();
+    bins.n_mid = g->n_pr_mid;
+    bins.big = g->d_pr_big.as<uint32_t>();
+    bins.n_big = g->n_pr_big;
+    bins.items = g->d_pr_items.as<uint2>();
+    bins.n_items = g->n_pr_items;
+    bins.longs = g->d_pr_longs.as<uint2>();
+    bins.n_longs = g->n_pr_longs;
+    bins.partial = ws.aux.as<float2>();
     for (uint32_t it = 0; it < iters; it++) {
         int cin = it & 1, cout = cin ^ 1;
         PTG_CUDA_TRY(cudaMemsetAsync(&dang[cout], 0, 8, st));
-        PTG_CUDA_TRY(cudaMemsetAsync(split_count, 0, 4, st));
         PrArgs a;
         a.n = n;
         a.m = m;
         a.off = off;
         a.col = g->d_col.as<uint32_t>();
-        a.tiles = tiles;
         a.contrib_in = contrib[cin];
         a.contrib_out = contrib[cout];
         a.rank_out = (it + 1 == iters) ? d_rank : nullptr;
-        a.acc = acc;
-        a.split_rows = ws.q[0].as<uint32_t>();
-        a.split_count = split_count;
-        a.split_cap = split_cap;
         a.dangling_in = &dang[cin];
         a.dangling_out = &dang[cout];
         a.d = damping;
         a.personalized = personalized ? 1 : 0;
         a.src = src;
-        launch(ctx, "k_spmv", k_spmv<OffT>, grid, kBlock, 0, st, a);
-        launch(ctx, "k_fixup", k_fixup<OffT>, sms * 2, kBlock, 0, st, a);
+        launch(ctx, "k_pr_small", k_pr_small<OffT>, fill_grid, kBlock, 0, st, a);
+        if (bins.n_mid)
+            launch(ctx, "k_pr_mid", k_pr_mid<OffT>, grid_for(bins.n_mid * 8, kBlock, sms * 8), kBlock, 0, st, a,
+                   bins);
+        if (bins.n_big)
+            launch(ctx, "k_pr_big", k_pr_big<OffT>, grid_for(bins.n_big * 32, kBlock, sms * 8), kBlock, 0, st, a,
+                   bins);
+        if (bins.n_items) {
+            launch(ctx, "k_pr_chunks", k_pr_chunks<OffT>, grid_for(bins.n_items * 32, kBlock, sms * 8), kBlock,
+                   0, st, a, bins);
+            launch(ctx, "k_pr_long", k_pr_long<OffT>, grid_for(bins.n_longs, kBlock, sms * 2), kBlock, 0, st, a,
+                   bins);
+        }
         PTG_CUDA_TRY(cudaGetLastError());
         rr.edges_relaxed += m;
     }
     rr.iterations = iters;
 }
 
-template <class OffT>
-void build_merge_tiles(ptg_graph *g) {
-    uint64_t ntiles = (g->n + g->m + kPrTile - 1) / kPrTile;
-    g->d_tiles.ensure((ntiles + 1) * 8);
-    launch(g->ctx, "k_merge_tiles", k_merge_tiles<OffT>, grid_for(ntiles + 1, kBlock, g->ctx->sm_count * 8),
-           kBlock, 0, g->ctx->stream, g->d_off.as<OffT>(), g->n, g->m, ntiles, g->d_tiles.as<uint64_t>());
-    PTG_CUDA_TRY(cudaGetLastError());
-}
-
 }  // namespace
 
-// Merge-path tile table of the resident graph (row index at each 1792-item
-// tile start), built on first use and kept with the graph.
-const uint64_t *merge_tiles(ptg_graph *g) {
-    if (!g->d_tiles.p) {
-        if (g->off64) build_merge_tiles<unsigned long long>(g);
-        else build_merge_tiles<uint32_t>(g);
-    }
-    return g->d_tiles.as<uint64_t>();
+// Degree bins of a resident graph, built now rather than on first use.
+void pr_prepare_graph(ptg_graph *g) {
+    if (g->out_of_core || !g->symmetric || g->pr_bins_built) return;
+    if (g->off64) build_pr_bins<unsigned long long>(g);
+    else build_pr_bins<uint32_t>(g);
 }
-
-int merge_tile_items() { return kPrTile; }
 
 void run_pagerank(ptg_graph *g, bool personalized, uint32_t src, double damping, uint32_t iters,
                   float *d_rank, RunResult &rr) {

@@ -231,12 +231,14 @@ struct ptg_graph {
     bool symmetric = false, weighted = false, off64 = false;
     // device copies
     ptg::DevBuf d_off, d_col, d_w, d_invdeg;
-    ptg::DevBuf d_tiles;  // merge-path tile table (PageRank, CC), built on first use
     ptg::DevBuf d_nzbm;   // bitmap of vertices with edges (bottom-up BFS), built on first use
     double mean_weight = 0;  // mean resident edge weight (SSSP bucket width), measured on first use
     ptg::DevBuf d_pull_items;  // (vertex, chunk) work items of high-degree vertices (multi-source pull)
     uint64_t n_pull_items = 0;
     bool pull_items_built = false;
+    ptg::DevBuf d_pr_mid, d_pr_big, d_pr_items, d_pr_longs;  // PageRank rows binned by degree
+    uint64_t n_pr_mid = 0, n_pr_big = 0, n_pr_items = 0, n_pr_longs = 0;
+    bool pr_bins_built = false;
     ptg::DevBuf d_ppr_items, d_ppr_longs;  // long-row chunks (multi-source PPR)
     uint64_t n_ppr_items = 0, n_ppr_longs = 0;
     bool ppr_items_built = false;
@@ -248,6 +250,8 @@ struct ptg_graph {
     std::vector<uint64_t> part_first_vertex;  // [P+1]
     ptg::DevBuf d_part_first_vertex;
     const uint32_t *h_col = nullptr, *h_w = nullptr;  // pinned host edge arrays
+    // page-locked address range of h_col / h_w (bytes outside it are pageable)
+    uintptr_t pin_lo[2] = {0, 0}, pin_hi[2] = {~(uintptr_t)0, ~(uintptr_t)0};
     std::vector<void *> registered;                    // cudaHostRegister'ed ranges
     ptg::PinnedBuf own_col, own_w;                     // owned pinned copies
     ptg::DevBuf stage_col[3], stage_w[3];
@@ -270,6 +274,9 @@ constexpr int kItems = 8;
 constexpr int kTile = kBlock * kItems;  // edges per expand tile
 
 void set_error(ptg_ctx *ctx, const Error &e);
+// Host->device copy of streamed edges [e0, e1) of h_col (which = 0) or h_w
+// (which = 1), split so that no single copy mixes page-locked and pageable bytes.
+void stream_edges(ptg_graph *g, int which, void *dst, uint64_t e0, uint64_t e1, cudaStream_t cs);
 ptg_status guard(ptg_ctx *ctx, const std::function<void()> &fn);
 
 // kernel-side entry points (defined in the .cu files)
@@ -291,9 +298,8 @@ void run_msbfs(ptg_graph *g, const uint32_t *sources, uint32_t k, uint32_t *out,
 void run_cc_batch(ptg_ctx *ctx, uint32_t num_graphs, const uint64_t *vtx_begin,
                   const uint64_t *offsets, const uint32_t *col, uint32_t *labels, RunResult &rr);
 int sm_count_of(ptg_ctx *ctx);
-// Merge-path tiling of a resident graph's n row ends + m edges into tiles of
-// merge_tile_items() items; entry t is the row index at tile t's first item.
-const uint64_t *merge_tiles(ptg_graph *g);
-int merge_tile_items();
+// Builds a resident symmetric graph's PageRank degree bins now rather than on
+// first use.
+void pr_prepare_graph(ptg_graph *g);
 
 }  // namespace ptg

@@ -117,7 +117,10 @@ ptg_graph *make_view(ptg_graph *g, ptg_ctx *lane) {
     alias(v->d_off, g->d_off);
     alias(v->d_col, g->d_col);
     alias(v->d_w, g->d_w);
-    alias(v->d_tiles, g->d_tiles);
+    alias(v->d_pr_mid, g->d_pr_mid);
+    alias(v->d_pr_big, g->d_pr_big);
+    alias(v->d_pr_items, g->d_pr_items);
+    alias(v->d_pr_longs, g->d_pr_longs);
     alias(v->d_nzbm, g->d_nzbm);
     alias(v->d_pull_items, g->d_pull_items);
     alias(v->d_ppr_items, g->d_ppr_items);
@@ -127,6 +130,11 @@ ptg_graph *make_view(ptg_graph *g, ptg_ctx *lane) {
     v->n_ppr_items = g->n_ppr_items;
     v->n_ppr_longs = g->n_ppr_longs;
     v->ppr_items_built = g->ppr_items_built;
+    v->n_pr_mid = g->n_pr_mid;
+    v->n_pr_big = g->n_pr_big;
+    v->n_pr_items = g->n_pr_items;
+    v->n_pr_longs = g->n_pr_longs;
+    v->pr_bins_built = g->pr_bins_built;
     v->mean_weight = g->mean_weight;
     v->resident_edges = g->resident_edges;
     v->device_bytes = 0;
@@ -144,7 +152,10 @@ void drop_view(ptg_graph *v, const ptg_graph *g) {
     detach(v->d_off, g->d_off);
     detach(v->d_col, g->d_col);
     detach(v->d_w, g->d_w);
-    detach(v->d_tiles, g->d_tiles);
+    detach(v->d_pr_mid, g->d_pr_mid);
+    detach(v->d_pr_big, g->d_pr_big);
+    detach(v->d_pr_items, g->d_pr_items);
+    detach(v->d_pr_longs, g->d_pr_longs);
     detach(v->d_nzbm, g->d_nzbm);
     detach(v->d_pull_items, g->d_pull_items);
     detach(v->d_ppr_items, g->d_ppr_items);
@@ -343,7 +354,7 @@ ptg_status register_entry(ptg_server *s, ptg_graph *g, bool owned, uint32_t *gra
                 PTG_CUDA_TRY(cudaSetDevice(g->ctx->device));
                 trav_prepare_graph(g);
                 if (g->symmetric) {
-                    merge_tiles(g);
+                    pr_prepare_graph(g);
                     ms_prepare_graph(g);
                     ppr_prepare_graph(g);
                 }

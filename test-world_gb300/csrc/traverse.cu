@@ -691,12 +691,10 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
                         PTG_CUDA_TRY(cudaEventRecord(g->link_ev[0], cs));
                         link_open = true;
                     }
-                    PTG_CUDA_TRY(cudaMemcpyAsync(g->stage_col[b].p, g->h_col + e0, (e1 - e0) * 4,
-                                                 cudaMemcpyHostToDevice, cs));
+                    stream_edges(g, 0, g->stage_col[b].p, e0, e1, cs);
                     rr.link_bytes += (e1 - e0) * 4;
                     if (kind == TRAV_SSSP) {
-                        PTG_CUDA_TRY(cudaMemcpyAsync(g->stage_w[b].p, g->h_w + e0, (e1 - e0) * 4,
-                                                     cudaMemcpyHostToDevice, cs));
+                        stream_edges(g, 1, g->stage_w[b].p, e0, e1, cs);
                         rr.link_bytes += (e1 - e0) * 4;
                     }
                     PTG_CUDA_TRY(cudaEventRecord(g->stage_ready[b], cs));
