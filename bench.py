@@ -36,7 +36,7 @@ FALLBACK_HBM_GBS = 6800.0
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the SpMV kernels of one
 # PageRank iteration (k_pr_small/mid/big/chunks/long) on RMAT scale 22:
 # 670.73 MB + 5.08 MB over n + m = 4,194,304 + 128,307,638 items
-PR_DRAM_BYTES_PER_ITEM = (670.732288e6 + 5.081856e6) / (4194304 + 128307638)
+PR_DRAM_BYTES_PER_ITEM = (670.733312e6 + 5.081856e6) / (4194304 + 128307638)
 
 
 def parse():

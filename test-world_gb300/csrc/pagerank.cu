@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(kBlock) k_pr_mid(PrArgs a, PrBins bins) {
 
 // One warp per row: lane j sums edges j, j+32, ... (four gathers in flight).
 template <class OffT>
-__global__ void __launch_bounds__(kBlock) k_pr_big(PrArgs a, PrBins bins) {
+__global__ void __launch_bounds__(kBlock, 8) k_pr_big(PrArgs a, PrBins bins) {
     const OffT *off = reinterpret_cast<const OffT *>(a.off);
     const PrConst c = pr_const(a);
     const unsigned lane = lane_id();
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(kBlock) k_pr_big(PrArgs a, PrBins bins) {
 
 // Chunks of rows longer than kPrChunk: one warp per chunk, partial sums out.
 template <class OffT>
-__global__ void __launch_bounds__(kBlock) k_pr_chunks(PrArgs a, PrBins bins) {
+__global__ void __launch_bounds__(kBlock, 8) k_pr_chunks(PrArgs a, PrBins bins) {
     const OffT *off = reinterpret_cast<const OffT *>(a.off);
     const unsigned lane = lane_id();
     const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;

@@ -278,32 +278,36 @@ __global__ void k_nonzero_bits(const OffT *off, uint64_t n, uint32_t *nz) {
 }
 
 // Bottom-up BFS round (symmetric graphs): each unvisited vertex with edges
-// looks for a neighbour in the current frontier bitmap.  A warp takes 1024
-// consecutive vertices (32 bitmap words): it compacts the candidates
-// (non-zero degree, not yet visited) into a shared list so all lanes stay
-// busy, checks neighbours four at a time (four independent load chains per
-// step instead of one), and writes its 32 words of the next-frontier and
-// visited bitmaps with plain stores.
+// looks for a neighbour in the current frontier bitmap.  A warp takes 512
+// consecutive vertices (kBuWords = 16 bitmap words): it compacts the
+// candidates (non-zero degree, not yet visited) into a shared list so all
+// lanes stay busy, checks neighbours four at a time (four independent load
+// chains per step instead of one), and writes its words of the
+// next-frontier and visited bitmaps with plain stores.  16-word chunks keep
+// the list at 16 KB per CTA and the kernel at 32 registers, so 8 CTAs fit
+// an SM (32-word chunks: 6 CTAs, 1.9x slower on RMAT-24).
 constexpr int kBuWarps = kBlock / 32;
+constexpr int kBuWords = 16;
 template <class OffT>
-__global__ void __launch_bounds__(kBlock) k_bottom_up(uint64_t n, const OffT *off,
-                                                      const uint32_t *col, const uint32_t *bm_cur,
-                                                      const uint32_t *nz, PushTargets t) {
-    __shared__ uint32_t s_list[kBuWarps][1024];
+__global__ void __launch_bounds__(kBlock, 8) k_bottom_up(uint64_t n, const OffT *off,
+                                                         const uint32_t *col, const uint32_t *bm_cur,
+                                                         const uint32_t *nz, PushTargets t) {
+    __shared__ uint32_t s_list[kBuWarps][kBuWords * 32];
     __shared__ uint32_t s_found[kBuWarps][32];
     const uint32_t newval = t.ctl->level_val + 1u;
     const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
     const uint64_t words = (n + 31) / 32;
-    const uint64_t chunks = (words + 31) / 32;
+    const uint64_t chunks = (words + kBuWords - 1) / kBuWords;
     while (true) {
         // warps take chunks from a shared counter: chunk costs vary a lot
         uint64_t c = 0;
         if (lane == 0) c = atomicAdd(&t.ctl->bu_next, 1u);
         c = __shfl_sync(0xffffffffu, c, 0);
         if (c >= chunks) break;
-        uint64_t wd = c * 32 + lane;
+        uint64_t wd = c * kBuWords + lane;
+        bool mine = lane < (unsigned)kBuWords && wd < words;
         uint32_t visw = 0, cand = 0;
-        if (wd < words) {
+        if (mine) {
             visw = t.vis[wd];
             cand = nz[wd] & ~visw;
         }
@@ -336,12 +340,12 @@ __global__ void __launch_bounds__(kBlock) k_bottom_up(uint64_t n, const OffT *of
                         bit_test(bm_cur, c3);
             }
             if (found) {
-                atomicOr(&s_found[wid][(v >> 5) - (uint32_t)(c * 32)], 1u << (v & 31u));
+                atomicOr(&s_found[wid][(v >> 5) - (uint32_t)(c * kBuWords)], 1u << (v & 31u));
                 t.value[v] = newval;
             }
         }
         __syncwarp();
-        if (wd < words) {
+        if (mine) {
             uint32_t f = s_found[wid][lane];
             t.bm_next[wd] = f;
             if (f) t.vis[wd] = visw | f;
@@ -648,7 +652,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
             if (h_ctl->level_val != level_val) {
                 PTG_CUDA_TRY(cudaMemcpyAsync(&d_ctl->level_val, &level_val, 4, cudaMemcpyHostToDevice, st));
             }
-            launch(ctx, "k_bottom_up", k_bottom_up<OffT>, grid_for((words + 31) / 32, kBuWarps, sms * 6),
+            launch(ctx, "k_bottom_up", k_bottom_up<OffT>, grid_for((words + kBuWords - 1) / kBuWords, kBuWarps, sms * 8),
                    kBlock, 0, st, n, off, col, bm_cur, (const uint32_t *)g->d_nzbm.as<uint32_t>(), pt);
         } else {
             if (!small)
