@@ -301,7 +301,9 @@ typedef struct ptg_server_config {
                                      BFS 256, SSSP 64, PPR 32 (1 disables batching)   */
     uint32_t queue_capacity;      /* queued requests before PTG_ERR_BUSY; 0 = 65536    */
     uint32_t ppr_iterations;      /* 0 = 20                                            */
-    uint32_t reserved;
+    uint32_t no_calibration;      /* 1: skip timing the graph's query kinds at
+                                     registration (fused-or-single choices then
+                                     follow the costs of served batches)             */
     double ppr_damping;           /* 0 = 0.85                                          */
     uint64_t memory_budget_bytes; /* graphs + lane workspaces; 0 = free HBM at
                                      creation minus 10%                                */

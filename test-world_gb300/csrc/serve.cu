@@ -59,9 +59,12 @@ struct Entry {
     bool owned = false;
     bool busy = false;                 // out-of-core graphs: one query at a time
     std::vector<ptg_graph *> views;    // per lane (resident graphs)
-    // measured cost per kind (moving averages, ms): one fused pass, and one
-    // single-source query; negative until first measured
-    double fused_ms[3] = {-1, -1, -1}, single_ms[3] = {-1, -1, -1};
+    // cost per kind (ms) of one single-source query, of one fused pass of up
+    // to 64 sources and of a full-width pass; measured once with the device
+    // otherwise idle when the graph is registered (calibrated), else moving
+    // averages of served batches; negative until known
+    double single_ms[3] = {-1, -1, -1}, fused64_ms[3] = {-1, -1, -1}, fused_ms[3] = {-1, -1, -1};
+    bool calibrated = false;
 };
 
 struct Req {
@@ -190,6 +193,7 @@ uint32_t kind_max(const ptg_server *s, uint32_t kind) {
 }
 
 struct Batch {
+    Entry *ent = nullptr;  // taken under the server lock (the graph list may grow meanwhile)
     uint32_t graph = 0, kind = 0;
     bool fused = false;  // one multi-source pass, else single-source queries in turn
     std::vector<uint64_t> ids;
@@ -224,8 +228,9 @@ bool take_batch(ptg_server *s, Batch &b) {
     if (e.g->out_of_core || k == 1) b.fused = false;
     else if (e.single_ms[kd] < 0) b.fused = false;
     else if (e.fused_ms[kd] < 0) b.fused = true;
-    else b.fused = e.fused_ms[kd] < k * e.single_ms[kd];
+    else b.fused = (k <= 64 && e.fused64_ms[kd] > 0 ? e.fused64_ms[kd] : e.fused_ms[kd]) < k * e.single_ms[kd];
     if (!b.fused) k = 1;
+    b.ent = &e;
     b.graph = best->first.first;
     b.kind = kd;
     for (uint32_t i = 0; i < k; i++) {
@@ -243,7 +248,7 @@ bool take_batch(ptg_server *s, Batch &b) {
 }
 
 ptg_status run_batch(ptg_server *s, Lane &L, size_t li, const Batch &b) {
-    Entry &e = *s->graphs[b.graph];
+    Entry &e = *b.ent;
     const uint32_t k = (uint32_t)b.ids.size();
     if (e.g->out_of_core) {
         // streamed graph: single-source path on the caller's context
@@ -309,7 +314,7 @@ void lane_loop(ptg_server *s, size_t li) {
             L.launches = nl;
             Entry &e = *s->graphs[b.graph];
             e.busy = false;
-            if (rs == PTG_OK && !e.g->out_of_core) {
+            if (rs == PTG_OK && !e.g->out_of_core && !e.calibrated) {
                 double ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
                 double &c = b.fused ? e.fused_ms[b.kind] : e.single_ms[b.kind];
                 double x = b.fused ? ms : ms / b.ids.size();
@@ -342,6 +347,63 @@ void lane_loop(ptg_server *s, size_t li) {
     }
 }
 
+// Times one single-source query and fused passes of 64 and of the full width
+// for every kind the graph serves, on lane 0 (sources: non-isolated vertices
+// spread over the first 2^20 ids).  Results go to one device scratch row.
+template <class OffT>
+void calibrate(ptg_server *s, uint32_t gid) {
+    Entry *ep;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        ep = s->graphs[gid].get();
+    }
+    Entry &e = *ep;
+    ptg_graph *g = e.g;
+    const uint64_t look = std::min<uint64_t>(g->n, 1ull << 20);
+    std::vector<OffT> off(look + 1);
+    PTG_CUDA_TRY(cudaSetDevice(g->ctx->device));
+    PTG_CUDA_TRY(cudaMemcpy(off.data(), g->d_off.p, (look + 1) * sizeof(OffT), cudaMemcpyDeviceToHost));
+    std::vector<uint32_t> cand;
+    for (uint64_t v = 0; v < look; v++)
+        if (off[v + 1] > off[v]) cand.push_back((uint32_t)v);
+    if (cand.empty()) return;
+    std::vector<uint32_t> src;
+    const uint32_t want = 256;
+    for (uint32_t i = 0; i < want; i++) src.push_back(cand[(uint64_t)i * cand.size() / want]);
+    DevBuf scratch;
+    scratch.ensure(g->n * 4);
+    auto run = [&](uint32_t kind, uint32_t k, bool fused) -> double {
+        Batch b;
+        b.ent = &e;
+        b.graph = gid;
+        b.kind = kind;
+        b.fused = fused;
+        for (uint32_t i = 0; i < k; i++) {
+            b.ids.push_back(0);
+            b.srcs.push_back(src[i % src.size()]);
+            b.results.push_back(scratch.p);
+        }
+        if (run_batch(s, *s->lanes[0], 0, b) != PTG_OK) return -1;  // warm-up: workspace growth
+        auto t0 = Clock::now();
+        if (run_batch(s, *s->lanes[0], 0, b) != PTG_OK) return -1;
+        return std::chrono::duration<double, std::milli>(Clock::now() - t0).count();
+    };
+    for (uint32_t kind = 0; kind < 3; kind++) {
+        if (kind == PTG_Q_SSSP && !g->weighted) continue;
+        if (kind == PTG_Q_PPR && !g->symmetric) continue;
+        uint32_t kmax = kind_max(s, kind);
+        double sm = run(kind, 1, false);
+        double f64 = kmax > 1 ? run(kind, std::min<uint32_t>(64, kmax), true) : -1;
+        double fm = kmax > 64 ? run(kind, kmax, true) : f64;
+        std::lock_guard<std::mutex> lk(s->mu);
+        e.single_ms[kind] = sm;
+        e.fused64_ms[kind] = f64;
+        e.fused_ms[kind] = fm;
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    e.calibrated = true;
+}
+
 ptg_status register_entry(ptg_server *s, ptg_graph *g, bool owned, uint32_t *graph_id) {
     auto e = std::make_unique<Entry>();
     e->g = g;
@@ -364,12 +426,24 @@ ptg_status register_entry(ptg_server *s, ptg_graph *g, bool owned, uint32_t *gra
         }
         for (auto &L : s->lanes) e->views.push_back(make_view(g, L->ctx));
     }
-    std::lock_guard<std::mutex> lk(s->mu);
-    if (owned) s->graph_bytes += g->device_bytes;
-    if (g->out_of_core) s->st.streamed_graphs++;
-    else s->st.resident_graphs++;
-    s->graphs.push_back(std::move(e));
-    *graph_id = (uint32_t)(s->graphs.size() - 1);
+    uint32_t gid;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (owned) s->graph_bytes += g->device_bytes;
+        if (g->out_of_core) s->st.streamed_graphs++;
+        else s->st.resident_graphs++;
+        s->graphs.push_back(std::move(e));
+        gid = (uint32_t)(s->graphs.size() - 1);
+    }
+    // no request can name the graph before its id is returned
+    if (!g->out_of_core && !s->cfg.no_calibration) {
+        ptg_status st = guard(g->ctx, [&] {
+            if (g->off64) calibrate<unsigned long long>(s, gid);
+            else calibrate<uint32_t>(s, gid);
+        });
+        (void)st;  // an uncalibrated graph falls back to measuring served batches
+    }
+    *graph_id = gid;
     return PTG_OK;
 }
 
