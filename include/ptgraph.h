@@ -383,6 +383,30 @@ void ptg_host_csr_free(ptg_host_csr *g);
 void ptg_free(void *p);
 
 /* ------------------------------------------------------------------------ */
+/* The reference's on-disk CSR files (host only).                           */
+/* ------------------------------------------------------------------------ */
+enum {
+    PTG_FILE_BCSR = 0,   /* u32 n, u32 m, u32 offsets[n], u32 col[m]
+                            (little-endian; ptGraph/main.cu:97-121, 2608-2616) */
+    PTG_FILE_BWCSR = 1,  /* u32 n, u32 m, u32 offsets[n], {u32 to, u32 weight}[m]
+                            (main.cu:451-475, 2575-2606)                        */
+    PTG_FILE_JAVA = 2,   /* big-endian u32 n, u64 m, u64 offsets[n], u32 col[m]
+                            (readGraphFromJava, main.cu:2479-2573)              */
+    PTG_FILE_BCSR64 = 3  /* u32 n, u64 m, u64 offsets[n], u32 col[m], little-
+                            endian: the .bcsr layout for m >= 2^32 (no
+                            reference counterpart)                             */
+};
+/* Read a CSR file into a host CSR (u64 offsets with sentinel; weights only
+ * for PTG_FILE_BWCSR), in pinned memory when pinned != 0.  Returns
+ * PTG_ERR_INVALID for an unreadable file, a size that does not match the
+ * header, offsets that decrease or exceed m, or a target >= n.  Free with
+ * ptg_host_csr_free. */
+ptg_status ptg_read_csr_file(const char *path, uint32_t format, int pinned, ptg_host_csr *out);
+/* Write a host CSR in one of the formats above (PTG_FILE_BWCSR needs
+ * weights; the 32-bit formats need m < 2^32). */
+ptg_status ptg_write_csr_file(const char *path, uint32_t format, const ptg_host_csr *csr);
+
+/* ------------------------------------------------------------------------ */
 /* Drop-in entry points: the reference's names and parameter lists          */
 /* (ptGraph/main.cu:30-56).  nodePointersI has testNumNodes entries (no     */
 /* sentinel); returns elapsed ms or -1 on error.                            */

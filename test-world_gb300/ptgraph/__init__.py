@@ -157,6 +157,8 @@ _SIGS = {
                                        ctypes.POINTER(ctypes.c_double)]),
     "ptg_server_drain": (ctypes.c_int, [_vp]),
     "ptg_server_stats_get": (ctypes.c_int, [_vp, ctypes.POINTER(ServerStats)]),
+    "ptg_read_csr_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint32, ctypes.c_int, ctypes.POINTER(HostCsr)]),
+    "ptg_write_csr_file": (ctypes.c_int, [ctypes.c_char_p, ctypes.c_uint32, ctypes.POINTER(HostCsr)]),
     "ptg_gen_rmat": (ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_double, ctypes.c_double,
                                     ctypes.c_double, ctypes.c_uint64, ctypes.c_int, ctypes.c_uint32,
                                     ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
@@ -556,6 +558,30 @@ def gen_rmat(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1, symmetric=Tr
     _check(lib().ptg_gen_rmat(scale, edge_factor, a, b, c, seed, 1 if symmetric else 0, wmin, wmax,
                               threads, 0, ctypes.byref(hc)))
     return _take(hc, wmax > 0)
+
+
+PTG_FILE_BCSR, PTG_FILE_BWCSR, PTG_FILE_JAVA, PTG_FILE_BCSR64 = 0, 1, 2, 3
+
+
+def read_csr(path, fmt):
+    """Read a CSR file (PTG_FILE_*): (offsets u64 n+1, col u32, weight u32 or None)."""
+    hc = HostCsr()
+    _check(lib().ptg_read_csr_file(os.fsencode(path), fmt, 0, ctypes.byref(hc)))
+    return _take(hc, fmt == PTG_FILE_BWCSR)
+
+
+def write_csr(path, fmt, offsets, col, weight=None):
+    """Write a sentinel-form CSR (offsets n+1) in one of the PTG_FILE_* formats."""
+    off = np.ascontiguousarray(offsets, dtype=np.uint64)
+    col = np.ascontiguousarray(col, dtype=np.uint32)
+    w = None if weight is None else np.ascontiguousarray(weight, dtype=np.uint32)
+    hc = HostCsr()
+    hc.n, hc.m = off.size - 1, col.size
+    hc.offsets = off.ctypes.data_as(_u64p)
+    hc.col = col.ctypes.data_as(_u32p)
+    hc.weight = w.ctypes.data_as(_u32p) if w is not None else None
+    hc.pinned = 0
+    _check(lib().ptg_write_csr_file(os.fsencode(path), fmt, ctypes.byref(hc)))
 
 
 def gen_er_batch(num_graphs, nmin, nmax, avg_degree, seed=1, threads=0):
