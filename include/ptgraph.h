@@ -111,7 +111,9 @@ enum {
     PTG_RESIDENT_PREFIX = 0, /* lowest-numbered partitions stay in HBM (the
                                 reference's static prefix, main.cu:1222-1232) */
     PTG_RESIDENT_NONE = 1,   /* stream every partition (tests the swapper)     */
-    PTG_RESIDENT_HOT = 2     /* promote partitions by visit count
+    PTG_RESIDENT_HOT = 2     /* no static prefix: the device budget is a cache
+                                of partitions promoted by their visit counts
+                                and kept across traversals of the graph
                                 (gpu_kernels.cu:254-282, 475-485)              */
 };
 
@@ -122,7 +124,10 @@ typedef struct ptg_partition_config {
     uint32_t n_staging_buffers;   /* 2 or 3 (double/triple buffering); 0 = 2          */
     uint32_t resident_policy;     /* PTG_RESIDENT_*                                   */
     uint32_t force_out_of_core;   /* 1 = partition even if the graph fits             */
-    uint32_t hot_threshold;       /* PTG_RESIDENT_HOT promotion threshold (visits)    */
+    uint32_t hot_threshold;       /* PTG_RESIDENT_HOT: a partition is hot once the
+                                     edges of frontier vertices seen in it exceed
+                                     hot_threshold per 4096 of its edges (the
+                                     reference's 3600 per 4096-edge fragment)       */
 } ptg_partition_config;
 
 void ptg_partition_config_default(ptg_partition_config *cfg);
@@ -149,6 +154,7 @@ typedef struct ptg_run_stats {
     uint64_t link_bytes;        /* bytes streamed host->device by the swapper      */
     uint64_t partitions_streamed;
     uint64_t partitions_skipped;/* streamed partitions skipped as inactive         */
+    uint64_t partitions_cached; /* active partitions served from the hot cache     */
     double device_ms;           /* GPU time of the run (CUDA events)              */
     double link_ms;             /* time the copy stream was busy                   */
 } ptg_run_stats;

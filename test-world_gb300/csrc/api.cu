@@ -327,6 +327,11 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
         uint64_t usable = dfree > reserve ? dfree - reserve : 0;
         uint64_t P, R, PE;
         plan(g->n, g->m, off.data(), bpe, &cfg, usable, P, R, PE, &g->part_first_vertex);
+        if (cfg.resident_policy == PTG_RESIDENT_HOT && R < P) {
+            // the device budget holds a cache of hot partitions instead of a prefix
+            g->cache_slots = (uint32_t)R;
+            R = 0;
+        }
         g->num_partitions = P;
         g->resident_partitions = R;
         g->partition_edges = PE;
@@ -449,6 +454,17 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
             }
             g->device_bytes += (uint64_t)g->n_stage * PE * bpe;
             g->part_visits.assign(P, 0);
+            if (g->cache_slots) {
+                g->slots.reset(new HotSlot[g->cache_slots]);
+                for (uint32_t i = 0; i < g->cache_slots; i++) {
+                    PTG_CUDA_TRY(cudaEventCreateWithFlags(&g->slots[i].ready, cudaEventDisableTiming));
+                    PTG_CUDA_TRY(cudaEventCreateWithFlags(&g->slots[i].freed, cudaEventDisableTiming));
+                }
+                g->slot_of.assign(P, -1);
+                g->d_part_hits.ensure(P * 8);
+                g->h_part_hits.ensure(P * 8);
+                g->device_bytes += (uint64_t)g->cache_slots * PE * bpe;  // taken as partitions turn hot
+            }
         }
     });
     if (s != PTG_OK) {
@@ -490,6 +506,7 @@ void fill_stats(ptg_run_stats *st, const RunResult &rr) {
     st->link_bytes = rr.link_bytes;
     st->partitions_streamed = rr.parts_streamed;
     st->partitions_skipped = rr.parts_skipped;
+    st->partitions_cached = rr.parts_cached;
     st->device_ms = rr.device_ms;
     st->link_ms = rr.link_ms;
 }

@@ -19,6 +19,7 @@
 
 #include <atomic>
 #include <functional>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -225,6 +226,20 @@ struct ptg_ctx {
     ptg::Workspace ws;
 };
 
+namespace ptg {
+// A device slot of the hot-partition cache.
+struct HotSlot {
+    DevBuf col, w;
+    int64_t part = -1;  // cached partition, -1: free
+    bool has_col = false, has_w = false;
+    cudaEvent_t ready = nullptr, freed = nullptr;  // copy done / last relax done
+    ~HotSlot() {
+        if (ready) cudaEventDestroy(ready);
+        if (freed) cudaEventDestroy(freed);
+    }
+};
+}  // namespace ptg
+
 struct ptg_graph {
     ptg_ctx *ctx = nullptr;
     uint64_t n = 0, m = 0;
@@ -263,7 +278,12 @@ struct ptg_graph {
     // hot-partition residency
     uint32_t resident_policy = PTG_RESIDENT_PREFIX;
     uint32_t hot_threshold = 3600;
-    std::vector<uint64_t> part_visits;
+    std::vector<uint64_t> part_visits;   // edges of frontier vertices seen per partition
+    uint32_t cache_slots = 0;             // hot-partition cache size (PTG_RESIDENT_HOT)
+    std::unique_ptr<ptg::HotSlot[]> slots;
+    std::vector<int> slot_of;             // [P] slot of a cached partition, -1 if none
+    ptg::DevBuf d_part_hits;              // u64[P] per level (k_mark_partitions)
+    ptg::PinnedBuf h_part_hits;
 };
 
 namespace ptg {
@@ -282,7 +302,7 @@ ptg_status guard(ptg_ctx *ctx, const std::function<void()> &fn);
 // kernel-side entry points (defined in the .cu files)
 struct RunResult {
     uint32_t iterations = 0, bottom_up_rounds = 0;
-    uint64_t edges_relaxed = 0, link_bytes = 0, parts_streamed = 0, parts_skipped = 0;
+    uint64_t edges_relaxed = 0, link_bytes = 0, parts_streamed = 0, parts_skipped = 0, parts_cached = 0;
     double device_ms = 0, link_ms = 0;
 };
 

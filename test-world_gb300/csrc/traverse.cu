@@ -288,6 +288,7 @@ __global__ void k_nonzero_bits(const OffT *off, uint64_t n, uint32_t *nz) {
 // an SM (32-word chunks: 6 CTAs, 1.9x slower on RMAT-24).
 constexpr int kBuWarps = kBlock / 32;
 constexpr int kBuWords = 16;
+constexpr uint64_t kHotSmemParts = 4096;  // partitions counted in shared memory by k_mark_partitions
 template <class OffT>
 __global__ void __launch_bounds__(kBlock, 8) k_bottom_up(uint64_t n, const OffT *off,
                                                          const uint32_t *col, const uint32_t *bm_cur,
@@ -360,7 +361,17 @@ __global__ void __launch_bounds__(kBlock, 8) k_bottom_up(uint64_t n, const OffT 
 template <class OffT>
 __global__ void k_mark_partitions(const uint32_t *q, const TravCtl *ctl, const OffT *off,
                                   uint64_t resident_edges, uint64_t part_edges,
-                                  uint64_t resident_parts, uint64_t nparts, uint8_t *flags) {
+                                  uint64_t resident_parts, uint64_t nparts, uint8_t *flags,
+                                  unsigned long long *hits) {
+    // hits (hot-partition cache only): edges of frontier vertices per
+    // partition this level, summed per CTA in shared memory when the
+    // partition count allows (the dynamic shared size is then nparts * 8)
+    extern __shared__ unsigned long long s_hits[];
+    const bool local = hits != nullptr && nparts <= kHotSmemParts;
+    if (local) {
+        for (uint64_t i = threadIdx.x; i < nparts; i += blockDim.x) s_hits[i] = 0;
+        __syncthreads();
+    }
     uint64_t F = ctl->F;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < F;
          i += (uint64_t)gridDim.x * blockDim.x) {
@@ -369,8 +380,19 @@ __global__ void k_mark_partitions(const uint32_t *q, const TravCtl *ctl, const O
         if (e <= resident_edges || e <= b) continue;
         if (b < resident_edges) b = resident_edges;
         uint64_t p0 = b / part_edges, p1 = (e - 1) / part_edges;
-        for (uint64_t p = p0; p <= p1 && p < nparts; p++)
+        for (uint64_t p = p0; p <= p1 && p < nparts; p++) {
             if (p >= resident_parts && !flags[p]) flags[p] = 1;
+            if (hits) {
+                uint64_t lo = max(b, p * part_edges), hi = min(e, (p + 1) * part_edges);
+                if (local) atomicAdd(&s_hits[p], (unsigned long long)(hi - lo));
+                else atomicAdd(&hits[p], (unsigned long long)(hi - lo));
+            }
+        }
+    }
+    if (local) {
+        __syncthreads();
+        for (uint64_t i = threadIdx.x; i < nparts; i += blockDim.x)
+            if (s_hits[i]) atomicAdd(&hits[i], s_hits[i]);
     }
 }
 
@@ -462,6 +484,42 @@ __global__ void __launch_bounds__(kBlock) k_far_split(uint32_t *far_bm, uint64_t
             bm[wd] |= moved;
         }
     }
+}
+
+// Hot-partition cache (the reference's visit-counted fragment promotion,
+// gpu_kernels.cu:254-282 and 475-485, where a 4096-edge fragment whose visit
+// record exceeds 3600 becomes a swap candidate).  part_visits[p] accumulates
+// the edges of frontier vertices that fell in partition p; a partition is hot
+// once that exceeds hot_threshold visits per 4096 edges.  A hot partition
+// takes a free slot, or the slot of the coldest cached partition if that one
+// has fewer visits; a cached partition is relaxed from its slot without a
+// copy, in this and every later traversal of the graph.  Returns the slot,
+// or -1 to use a staging buffer.
+int hot_slot(ptg_graph *g, uint64_t p, uint64_t edges) {
+    if (g->slot_of[p] >= 0) return g->slot_of[p];
+    if ((double)g->part_visits[p] * 4096.0 <= (double)g->hot_threshold * (double)edges) return -1;
+    int victim = -1;
+    for (uint32_t s = 0; s < g->cache_slots; s++) {
+        int64_t q = g->slots[s].part;
+        if (q < 0) {
+            victim = (int)s;
+            break;
+        }
+        if (victim < 0 || g->part_visits[q] < g->part_visits[g->slots[victim].part]) victim = (int)s;
+    }
+    if (victim < 0) return -1;
+    HotSlot &hs = g->slots[victim];
+    if (hs.part >= 0) {
+        if (g->part_visits[hs.part] >= g->part_visits[p]) return -1;
+        g->slot_of[hs.part] = -1;
+    }
+    uint64_t bytes = g->partition_edges * 4;
+    hs.col.ensure(bytes);
+    if (g->weighted) hs.w.ensure(bytes);
+    hs.part = (int64_t)p;
+    hs.has_col = hs.has_w = false;
+    g->slot_of[p] = victim;
+    return victim;
 }
 
 // ---------------------------------------------------------------------------
@@ -672,14 +730,23 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
             PTG_CUDA_TRY(cudaGetLastError());
             if (g->out_of_core) {
                 // stream the active partitions past the resident prefix
+                const bool hot = g->cache_slots > 0;
                 uint8_t *d_flags = ws.flags.as<uint8_t>();
+                unsigned long long *d_hits = hot ? g->d_part_hits.as<unsigned long long>() : nullptr;
                 PTG_CUDA_TRY(cudaMemsetAsync(d_flags, 0, g->num_partitions, st));
+                if (hot) PTG_CUDA_TRY(cudaMemsetAsync(d_hits, 0, g->num_partitions * 8, st));
+                size_t hsm = hot && g->num_partitions <= kHotSmemParts ? g->num_partitions * 8 : 0;
                 launch(ctx, "k_mark_partitions", k_mark_partitions<OffT>, grid_for(F, kBlock, sms * 8), kBlock,
-                       0, st, q_cur, d_ctl, off, g->resident_edges, g->partition_edges,
-                       g->resident_partitions, g->num_partitions, d_flags);
+                       hsm, st, q_cur, d_ctl, off, g->resident_edges, g->partition_edges,
+                       g->resident_partitions, g->num_partitions, d_flags, d_hits);
                 PTG_CUDA_TRY(cudaMemcpyAsync(h_flags, d_flags, g->num_partitions, cudaMemcpyDeviceToHost, st));
+                if (hot)
+                    PTG_CUDA_TRY(cudaMemcpyAsync(g->h_part_hits.p, d_hits, g->num_partitions * 8,
+                                                 cudaMemcpyDeviceToHost, st));
                 PTG_CUDA_TRY(cudaStreamSynchronize(st));
                 link_open = false;
+                const bool need_w = kind == TRAV_SSSP;
+                cudaStream_t cs = ctx->copy_stream;
                 for (uint64_t p = g->resident_partitions; p < g->num_partitions; p++) {
                     if (!h_flags[p]) {
                         rr.parts_skipped++;
@@ -687,26 +754,60 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
                     }
                     uint64_t e0 = p * g->partition_edges;
                     uint64_t e1 = std::min<uint64_t>(g->m, e0 + g->partition_edges);
-                    int b = stage_next;
-                    stage_next = (stage_next + 1) % (int)g->n_stage;
-                    cudaStream_t cs = ctx->copy_stream;
-                    PTG_CUDA_TRY(cudaStreamWaitEvent(cs, g->stage_free[b], 0));
-                    if (!link_open) {
-                        PTG_CUDA_TRY(cudaEventRecord(g->link_ev[0], cs));
-                        link_open = true;
+                    const uint32_t *sc_ = nullptr, *sw_ = nullptr;
+                    int slot = -1;
+                    if (hot) {
+                        g->part_visits[p] += g->h_part_hits.as<unsigned long long>()[p];
+                        slot = hot_slot(g, p, e1 - e0);
                     }
-                    stream_edges(g, 0, g->stage_col[b].p, e0, e1, cs);
-                    rr.link_bytes += (e1 - e0) * 4;
-                    if (kind == TRAV_SSSP) {
-                        stream_edges(g, 1, g->stage_w[b].p, e0, e1, cs);
-                        rr.link_bytes += (e1 - e0) * 4;
+                    // a partition copies into a cache slot (kept for later levels and
+                    // queries) or into the next staging buffer
+                    bool copy_col = true, copy_w = need_w;
+                    void *dcol, *dw;
+                    cudaEvent_t ready, freed;
+                    if (slot >= 0) {
+                        HotSlot &hs = g->slots[slot];
+                        copy_col = !hs.has_col;
+                        copy_w = need_w && !hs.has_w;
+                        dcol = hs.col.p;
+                        dw = hs.w.p;
+                        ready = hs.ready;
+                        freed = hs.freed;
+                        if (!copy_col && !copy_w) rr.parts_cached++;
+                    } else {
+                        int b = stage_next;
+                        stage_next = (stage_next + 1) % (int)g->n_stage;
+                        dcol = g->stage_col[b].p;
+                        dw = g->stage_w[b].p;
+                        ready = g->stage_ready[b];
+                        freed = g->stage_free[b];
                     }
-                    PTG_CUDA_TRY(cudaEventRecord(g->stage_ready[b], cs));
-                    PTG_CUDA_TRY(cudaStreamWaitEvent(st, g->stage_ready[b], 0));
+                    if (copy_col || copy_w) {
+                        PTG_CUDA_TRY(cudaStreamWaitEvent(cs, freed, 0));
+                        if (!link_open) {
+                            PTG_CUDA_TRY(cudaEventRecord(g->link_ev[0], cs));
+                            link_open = true;
+                        }
+                        if (copy_col) {
+                            stream_edges(g, 0, dcol, e0, e1, cs);
+                            rr.link_bytes += (e1 - e0) * 4;
+                        }
+                        if (copy_w) {
+                            stream_edges(g, 1, dw, e0, e1, cs);
+                            rr.link_bytes += (e1 - e0) * 4;
+                        }
+                        PTG_CUDA_TRY(cudaEventRecord(ready, cs));
+                        PTG_CUDA_TRY(cudaStreamWaitEvent(st, ready, 0));
+                        rr.parts_streamed++;
+                        if (slot >= 0) {
+                            g->slots[slot].has_col = true;
+                            g->slots[slot].has_w |= copy_w;
+                        }
+                    }
+                    sc_ = static_cast<const uint32_t *>(dcol);
+                    sw_ = static_cast<const uint32_t *>(dw);
                     uint64_t vf = g->part_first_vertex[p], vl = g->part_first_vertex[p + 1];
                     int pg = grid_for(e1 - e0, kTile, sms * 8);
-                    const uint32_t *sc_ = g->stage_col[b].as<uint32_t>();
-                    const uint32_t *sw_ = g->stage_w[b].as<uint32_t>();
                     if (kind == TRAV_BFS)
                         launch(ctx, "k_relax_partition_bfs", k_relax_partition<OffT, 0>, pg, kBlock, 0, st, e0,
                                e1, vf, vl, off, sc_, sw_, bm_cur, pt);
@@ -717,12 +818,9 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
                         launch(ctx, "k_relax_partition_cc", k_relax_partition<OffT, 2>, pg, kBlock, 0, st, e0,
                                e1, vf, vl, off, sc_, sw_, bm_cur, pt);
                     PTG_CUDA_TRY(cudaGetLastError());
-                    PTG_CUDA_TRY(cudaEventRecord(g->stage_free[b], st));
-                    rr.parts_streamed++;
-                    if (g->resident_policy == PTG_RESIDENT_HOT && p < g->part_visits.size())
-                        g->part_visits[p]++;
+                    PTG_CUDA_TRY(cudaEventRecord(freed, st));
                 }
-                if (link_open) PTG_CUDA_TRY(cudaEventRecord(g->link_ev[1], ctx->copy_stream));
+                if (link_open) PTG_CUDA_TRY(cudaEventRecord(g->link_ev[1], cs));
             }
         }
         // next frontier: queue from the bitmap

@@ -66,6 +66,7 @@ class RunStats(ctypes.Structure):
                 ("edges_relaxed", ctypes.c_uint64), ("vertices_reached", ctypes.c_uint64),
                 ("edges_in_component", ctypes.c_uint64), ("link_bytes", ctypes.c_uint64),
                 ("partitions_streamed", ctypes.c_uint64), ("partitions_skipped", ctypes.c_uint64),
+                ("partitions_cached", ctypes.c_uint64),
                 ("device_ms", ctypes.c_double), ("link_ms", ctypes.c_double)]
 
     def as_dict(self):

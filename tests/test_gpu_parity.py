@@ -291,3 +291,25 @@ def test_ppr_batch_long_rows_and_independence(ptg, ctx, oracle):
     assert np.array_equal(alone[0].view(np.uint32), pb[5].view(np.uint32))
     shuffled = G.ppr_batch(srcs[::-1].copy())
     assert np.array_equal(shuffled[::-1].view(np.uint32), pb.view(np.uint32))
+
+
+def test_hot_partition_cache(ptg, ctx, oracle):
+    """PTG_RESIDENT_HOT: no static prefix; partitions promoted by visit counts stay in
+    device slots across traversals, so a repeated search streams fewer bytes."""
+    off, col, w = ptg.gen_rmat(14, 16, seed=3, symmetric=False, wmin=1, wmax=63)
+    pb = max(64, (col.size * 8 // 16) // 8 * 8)  # about 16 partitions of weighted edges
+    cfg = ptg.partition_config(partition_bytes=pb, device_budget_bytes=pb * 9, force_out_of_core=1,
+                               n_staging_buffers=2, resident_policy=ptg.PTG_RESIDENT_HOT, hot_threshold=1)
+    G = ctx.graph(off, col, w, symmetric=False, config=cfg)
+    info = G.info()
+    assert info["out_of_core"] == 1 and info["resident_partitions"] == 0
+    assert (G.bfs(0) == oracle.bfs(off, col, 0, method="queue")).all()  # fills slots with columns only
+    ref = oracle.sssp(off, col, w, 0)
+    s1, s2 = {}, {}
+    assert (G.sssp(0, stats=s1) == ref).all()
+    assert (G.sssp(0, stats=s2) == ref).all()
+    assert s2["partitions_cached"] > 0 and s2["link_bytes"] < s1["link_bytes"]
+    for s in (5, 777, 16000):
+        assert (G.sssp(s) == oracle.sssp(off, col, w, s)).all()
+        assert (G.bfs(s) == oracle.bfs(off, col, s, method="queue")).all()
+    assert (G.cc() == oracle.cc(off, col)).all()
