@@ -111,10 +111,14 @@ enum {
     PTG_RESIDENT_PREFIX = 0, /* lowest-numbered partitions stay in HBM (the
                                 reference's static prefix, main.cu:1222-1232) */
     PTG_RESIDENT_NONE = 1,   /* stream every partition (tests the swapper)     */
-    PTG_RESIDENT_HOT = 2     /* no static prefix: the device budget is a cache
+    PTG_RESIDENT_HOT = 2,    /* no static prefix: the device budget is a cache
                                 of partitions promoted by their visit counts
                                 and kept across traversals of the graph
                                 (gpu_kernels.cu:254-282, 475-485)              */
+    PTG_RESIDENT_HUBS = 3    /* the device budget holds, fixed, the partitions
+                                with the most edges of the highest-degree
+                                vertices (the reference's degree-sorted
+                                placement, main.cu:2196-2394)                  */
 };
 
 typedef struct ptg_partition_config {

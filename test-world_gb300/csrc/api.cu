@@ -142,6 +142,50 @@ void plan(uint64_t n, uint64_t m, const uint64_t *off, uint64_t bpe, const ptg_p
     }
 }
 
+// PTG_RESIDENT_HUBS: rank partitions by the edges they hold of the
+// highest-degree vertices (vertices taken in decreasing degree until their
+// edges would fill the slots) and load the best into the slots now.
+void place_hubs(ptg_graph *g, const std::vector<uint64_t> &off, uint64_t PE, cudaStream_t st) {
+    const uint64_t n = g->n, P = g->num_partitions, budget = (uint64_t)g->cache_slots * PE;
+    std::vector<uint64_t> deg(n);
+    for (uint64_t v = 0; v < n; v++) deg[v] = off[v + 1] - off[v];
+    std::vector<uint64_t> sorted(deg);
+    std::sort(sorted.begin(), sorted.end(), std::greater<uint64_t>());
+    uint64_t cut = 0, acc = 0;  // smallest hub degree
+    for (uint64_t d : sorted) {
+        if (d == 0 || acc + d > budget) break;
+        acc += d;
+        cut = d;
+    }
+    std::vector<uint64_t> score(P, 0);
+    for (uint64_t v = 0; cut && v < n; v++) {
+        if (deg[v] < cut) continue;
+        for (uint64_t e = off[v]; e < off[v + 1];) {
+            uint64_t p = e / PE, hi = std::min(off[v + 1], (p + 1) * PE);
+            score[p] += hi - e;
+            e = hi;
+        }
+    }
+    std::vector<uint64_t> order(P);
+    for (uint64_t p = 0; p < P; p++) order[p] = p;
+    std::stable_sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) { return score[a] > score[b]; });
+    for (uint32_t s = 0; s < g->cache_slots && s < P && score[order[s]] > 0; s++) {
+        uint64_t p = order[s], e0 = p * PE, e1 = std::min(g->m, e0 + PE);
+        HotSlot &hs = g->slots[s];
+        hs.col.ensure(PE * 4);
+        stream_edges(g, 0, hs.col.p, e0, e1, st);
+        if (g->weighted) {
+            hs.w.ensure(PE * 4);
+            stream_edges(g, 1, hs.w.p, e0, e1, st);
+        }
+        hs.part = (int64_t)p;
+        hs.has_col = true;
+        hs.has_w = g->weighted;
+        g->slot_of[p] = (int)s;
+    }
+    PTG_CUDA_TRY(cudaStreamSynchronize(st));
+}
+
 }  // namespace
 }  // namespace ptg
 
@@ -327,9 +371,10 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
         uint64_t usable = dfree > reserve ? dfree - reserve : 0;
         uint64_t P, R, PE;
         plan(g->n, g->m, off.data(), bpe, &cfg, usable, P, R, PE, &g->part_first_vertex);
-        if (cfg.resident_policy == PTG_RESIDENT_HOT && R < P) {
-            // the device budget holds a cache of hot partitions instead of a prefix
+        if ((cfg.resident_policy == PTG_RESIDENT_HOT || cfg.resident_policy == PTG_RESIDENT_HUBS) && R < P) {
+            // the device budget holds partition slots instead of a prefix
             g->cache_slots = (uint32_t)R;
+            g->cache_static = cfg.resident_policy == PTG_RESIDENT_HUBS;
             R = 0;
         }
         g->num_partitions = P;
@@ -464,6 +509,7 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
                 g->d_part_hits.ensure(P * 8);
                 g->h_part_hits.ensure(P * 8);
                 g->device_bytes += (uint64_t)g->cache_slots * PE * bpe;  // taken as partitions turn hot
+                if (g->cache_static) place_hubs(g, off, PE, st);
             }
         }
     });

@@ -279,7 +279,8 @@ struct ptg_graph {
     uint32_t resident_policy = PTG_RESIDENT_PREFIX;
     uint32_t hot_threshold = 3600;
     std::vector<uint64_t> part_visits;   // edges of frontier vertices seen per partition
-    uint32_t cache_slots = 0;             // hot-partition cache size (PTG_RESIDENT_HOT)
+    uint32_t cache_slots = 0;             // partition slots in HBM (PTG_RESIDENT_HOT / _HUBS)
+    bool cache_static = false;            // slots filled at creation, no promotion (_HUBS)
     std::unique_ptr<ptg::HotSlot[]> slots;
     std::vector<int> slot_of;             // [P] slot of a cached partition, -1 if none
     ptg::DevBuf d_part_hits;              // u64[P] per level (k_mark_partitions)

@@ -497,6 +497,7 @@ __global__ void __launch_bounds__(kBlock) k_far_split(uint32_t *far_bm, uint64_t
 // or -1 to use a staging buffer.
 int hot_slot(ptg_graph *g, uint64_t p, uint64_t edges) {
     if (g->slot_of[p] >= 0) return g->slot_of[p];
+    if (g->cache_static) return -1;
     if ((double)g->part_visits[p] * 4096.0 <= (double)g->hot_threshold * (double)edges) return -1;
     int victim = -1;
     for (uint32_t s = 0; s < g->cache_slots; s++) {

@@ -25,7 +25,7 @@ PTG_ERR_UNSUPPORTED, PTG_ERR_NO_DEVICE, PTG_ERR_CANCELLED, PTG_ERR_BUSY = 5, 6, 
 PTG_OFFSETS_U32, PTG_OFFSETS_U64 = 0, 1
 PTG_FORM_SENTINEL, PTG_FORM_REFERENCE = 0, 1
 PTG_CSR_SYMMETRIC, PTG_CSR_HOST_PINNED = 1, 2
-PTG_RESIDENT_PREFIX, PTG_RESIDENT_NONE, PTG_RESIDENT_HOT = 0, 1, 2
+PTG_RESIDENT_PREFIX, PTG_RESIDENT_NONE, PTG_RESIDENT_HOT, PTG_RESIDENT_HUBS = 0, 1, 2, 3
 PTG_OUT_DEVICE, PTG_LEVEL_ZERO_BASED, PTG_UNREACHED_MINUS1 = 1, 2, 4
 PTG_NO_DIRECTION_OPT, PTG_REFERENCE_SCHEDULE = 8, 16
 PTG_Q_BFS, PTG_Q_SSSP, PTG_Q_PPR = 0, 1, 2

@@ -313,3 +313,23 @@ def test_hot_partition_cache(ptg, ctx, oracle):
         assert (G.sssp(s) == oracle.sssp(off, col, w, s)).all()
         assert (G.bfs(s) == oracle.bfs(off, col, s, method="queue")).all()
     assert (G.cc() == oracle.cc(off, col)).all()
+
+
+def test_hub_placement(ptg, ctx, oracle):
+    """PTG_RESIDENT_HUBS: the budget holds, from creation on, the partitions with the most
+    edges of the highest-degree vertices; they are never streamed."""
+    off, col, w = ptg.gen_rmat(14, 16, seed=3, symmetric=False, wmin=1, wmax=63)
+    pb = max(64, (col.size * 8 // 16) // 8 * 8)
+    base = dict(partition_bytes=pb, device_budget_bytes=pb * 6, force_out_of_core=1, n_staging_buffers=2)
+    G = ctx.graph(off, col, w, symmetric=False,
+                  config=ptg.partition_config(resident_policy=ptg.PTG_RESIDENT_HUBS, **base))
+    N = ctx.graph(off, col, w, symmetric=False,
+                  config=ptg.partition_config(resident_policy=ptg.PTG_RESIDENT_NONE, **base))
+    assert G.info()["resident_partitions"] == 0
+    sh, sn = {}, {}
+    ref = oracle.sssp(off, col, w, 0)
+    assert (G.sssp(0, stats=sh) == ref).all()
+    assert (N.sssp(0, stats=sn) == ref).all()
+    assert sh["partitions_cached"] > 0 and sh["link_bytes"] < sn["link_bytes"]
+    assert (G.bfs(0) == oracle.bfs(off, col, 0, method="queue")).all()
+    assert (G.cc() == oracle.cc(off, col)).all()
