@@ -246,9 +246,8 @@ ptg_status ptg_pagerank(ptg_graph *g, float *rank, const ptg_pr_opts *opts);
 /* Personalized PageRank: teleport (and dangling mass) to src, r0 = e_src. */
 ptg_status ptg_ppr(ptg_graph *g, uint32_t src, float *rank, const ptg_pr_opts *opts);
 /* Personalized PageRank for k sources: rank holds k rows of n floats, row i
- * the PPR of sources[i] (same semantics and tolerance as ptg_ppr; the
- * per-vertex sums run in a different order).  Sources run 32 per pass, and a
- * source's result does not depend on which other sources share its pass. */
+ * equal bit for bit to ptg_ppr(sources[i]) with the same options.  Sources
+ * run 8 per pass (4- or 8-wide values, one vector load per neighbour). */
 ptg_status ptg_ppr_batch(ptg_graph *g, const uint32_t *sources, uint32_t k, float *rank,
                          const ptg_pr_opts *opts);
 

@@ -294,6 +294,215 @@ __global__ void __launch_bounds__(kBlock) k_pr_long(PrArgs a, PrBins bins) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Personalized PageRank for K = 4 or 8 sources at once over the same degree
+// bins.  Values are vertex-major (x[v*K + s]), so a neighbour's K values are
+// one 16- or 32-byte vector load; every thread keeps K two-float sums and
+// walks the same edges in the same order as the single-source kernels above,
+// and partials meet through the same shuffles, so each source's ranks are
+// bit-identical to a single-source ptg_ppr of that source.
+// ---------------------------------------------------------------------------
+struct MsArgs {
+    uint64_t n;
+    const void *off;
+    const uint32_t *col;
+    const float *cin;       // [n*K]
+    float *cout;            // [n*K] contributions, or ranks on the last iteration
+    const double *dang_in;  // [K]
+    double *dang_out;       // [K], zero on entry
+    const uint32_t *src;    // [K] (0xFFFFFFFF: unused lane)
+    double d;
+    int last;
+};
+
+template <int K>
+__device__ __forceinline__ void ms_load(const float *x, uint32_t u, float (&v)[K]) {
+    const float4 *p = reinterpret_cast<const float4 *>(x + (uint64_t)u * K);
+#pragma unroll
+    for (int i = 0; i < K / 4; i++) {
+        float4 t = p[i];
+        v[4 * i] = t.x;
+        v[4 * i + 1] = t.y;
+        v[4 * i + 2] = t.z;
+        v[4 * i + 3] = t.w;
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void ms_add(ff (&acc)[K], const float (&v)[K]) {
+#pragma unroll
+    for (int s = 0; s < K; s++) acc[s] = ff_add(acc[s], v[s]);
+}
+
+template <class OffT, int K>
+__device__ __forceinline__ void ms_finalize(const MsArgs &a, uint64_t v, OffT deg, const ff (&sum)[K]) {
+    const ff cd = ff_of(a.d);
+    float out[K];
+#pragma unroll
+    for (int s = 0; s < K; s++) {
+        ff r = ff_add(ff{0.f, 0.f}, ff_mul(cd, sum[s]));
+        if (v == a.src[s]) r = ff_add(r, ff_of((1.0 - a.d) + a.d * a.dang_in[s]));
+        float rf = r.hi + r.lo;
+        out[s] = a.last ? rf : (deg == 0 ? 0.f : rf / (float)deg);
+        if (deg == 0 && rf != 0.f) atomicAdd(&a.dang_out[s], (double)rf);
+    }
+    float4 *o = reinterpret_cast<float4 *>(a.cout + v * K);
+#pragma unroll
+    for (int i = 0; i < K / 4; i++) o[i] = make_float4(out[4 * i], out[4 * i + 1], out[4 * i + 2], out[4 * i + 3]);
+}
+
+// Adds, in order, the values of the neighbours at edges k0, k0 + stride, ...
+// below e, with up to U column and vector loads in flight per step.
+template <int K, int U, class OffT>
+__device__ __forceinline__ void ms_run(const MsArgs &a, OffT k0, OffT e, uint32_t stride, ff (&acc)[K]) {
+    for (OffT k = k0; k < e; k += (OffT)(U * stride)) {
+        uint32_t u[U];
+#pragma unroll
+        for (int t = 0; t < U; t++) u[t] = k + (OffT)(t * stride) < e ? __ldcs(a.col + k + t * stride) : 0u;
+        float x[U][K];
+#pragma unroll
+        for (int t = 0; t < U; t++)
+            if (k + (OffT)(t * stride) < e) ms_load<K>(a.cin, u[t], x[t]);
+#pragma unroll
+        for (int t = 0; t < U; t++)
+            if (k + (OffT)(t * stride) < e) ms_add<K>(acc, x[t]);
+    }
+}
+
+template <int K>
+__device__ __forceinline__ void ms_shfl_add(ff (&acc)[K], int o, int width) {
+#pragma unroll
+    for (int s = 0; s < K; s++) acc[s] = ff_add(acc[s], ff_shfl_xor(acc[s], o, width));
+}
+
+template <class OffT, int K>
+__global__ void __launch_bounds__(kBlock) k_prk_small(MsArgs a) {
+    const OffT *off = reinterpret_cast<const OffT *>(a.off);
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < a.n; v += (uint64_t)gridDim.x * blockDim.x) {
+        OffT b = off[v], e = off[v + 1];
+        OffT deg = e - b;
+        if ((uint64_t)deg > kPrSmall) continue;
+        ff acc[K];
+#pragma unroll
+        for (int s = 0; s < K; s++) acc[s] = ff{0.f, 0.f};
+        ms_run<K, kPrSmall>(a, b, e, 1, acc);
+        ms_finalize<OffT, K>(a, v, deg, acc);
+    }
+}
+
+template <class OffT, int K>
+__global__ void __launch_bounds__(kBlock) k_prk_mid(MsArgs a, PrBins bins) {
+    const OffT *off = reinterpret_cast<const OffT *>(a.off);
+    const unsigned sub = threadIdx.x & 7u;
+    const uint64_t groups = (uint64_t)gridDim.x * blockDim.x / 8;
+    const uint64_t span = (bins.n_mid + 3) / 4 * 4;
+    for (uint64_t gi = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 8; gi < span; gi += groups) {
+        bool valid = gi < bins.n_mid;
+        uint32_t v = valid ? bins.mid[gi] : 0u;
+        OffT b = valid ? off[v] : (OffT)0, e = valid ? off[v + 1] : (OffT)0;
+        ff acc[K];
+#pragma unroll
+        for (int s = 0; s < K; s++) acc[s] = ff{0.f, 0.f};
+        ms_run<K, 4>(a, b + sub, e, 8, acc);
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) ms_shfl_add<K>(acc, o, 8);
+        if (valid && sub == 0) ms_finalize<OffT, K>(a, v, e - b, acc);
+    }
+}
+
+template <class OffT, int K>
+__global__ void __launch_bounds__(kBlock) k_prk_big(MsArgs a, PrBins bins) {
+    const OffT *off = reinterpret_cast<const OffT *>(a.off);
+    const unsigned lane = lane_id();
+    const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
+    for (uint64_t wi = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; wi < bins.n_big; wi += warps) {
+        uint32_t v = bins.big[wi];
+        OffT b = off[v], e = off[v + 1];
+        ff acc[K];
+#pragma unroll
+        for (int s = 0; s < K; s++) acc[s] = ff{0.f, 0.f};
+        ms_run<K, 4>(a, b + lane, e, 32, acc);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ms_shfl_add<K>(acc, o, 32);
+        if (lane == 0) ms_finalize<OffT, K>(a, v, e - b, acc);
+    }
+}
+
+template <class OffT, int K>
+__global__ void __launch_bounds__(kBlock) k_prk_chunks(MsArgs a, PrBins bins) {
+    const OffT *off = reinterpret_cast<const OffT *>(a.off);
+    const unsigned lane = lane_id();
+    const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
+    for (uint64_t it = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; it < bins.n_items; it += warps) {
+        uint2 item = bins.items[it];
+        OffT b = off[item.x] + (OffT)item.y * (OffT)kPrChunk;
+        OffT e = off[(uint64_t)item.x + 1];
+        if (e - b > (OffT)kPrChunk) e = b + (OffT)kPrChunk;
+        ff acc[K];
+#pragma unroll
+        for (int s = 0; s < K; s++) acc[s] = ff{0.f, 0.f};
+        ms_run<K, 4>(a, b + lane, e, 32, acc);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) ms_shfl_add<K>(acc, o, 32);
+        if (lane == 0)
+#pragma unroll
+            for (int s = 0; s < K; s++) bins.partial[it * K + s] = make_float2(acc[s].hi, acc[s].lo);
+    }
+}
+
+template <class OffT, int K>
+__global__ void __launch_bounds__(kBlock) k_prk_long(MsArgs a, PrBins bins) {
+    const OffT *off = reinterpret_cast<const OffT *>(a.off);
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < bins.n_longs;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        uint2 L = bins.longs[j];
+        OffT deg = off[(uint64_t)L.x + 1] - off[L.x];
+        uint32_t pieces = (uint32_t)(((uint64_t)deg + kPrChunk - 1) / kPrChunk);
+        ff acc[K];
+#pragma unroll
+        for (int s = 0; s < K; s++) acc[s] = ff{0.f, 0.f};
+        for (uint32_t i = 0; i < pieces; i++)
+#pragma unroll
+            for (int s = 0; s < K; s++) {
+                float2 p = bins.partial[((uint64_t)L.y + i) * K + s];
+                acc[s] = ff_add(acc[s], ff{p.x, p.y});
+            }
+        ms_finalize<OffT, K>(a, L.x, deg, acc);
+    }
+}
+
+// r0 = e_src per lane: contribution 1/deg(src) at the source, dangling 1 for
+// an isolated source (as k_pr_init for one source).
+template <class OffT, int K>
+__global__ void k_prk_init(const OffT *off, const uint32_t *src, float *c, double *dang) {
+    unsigned s = threadIdx.x;
+    if (s >= (unsigned)K) return;
+    uint32_t v = src[s];
+    dang[s] = 0.0;
+    if (v == 0xFFFFFFFFu) return;
+    OffT deg = off[(uint64_t)v + 1] - off[v];
+    if (deg == 0) dang[s] = 1.0;
+    else c[(uint64_t)v * K + s] = 1.f / (float)deg;
+}
+
+// rank[v*K + s] -> out[s*n + v] for s < k (32 vertices x K sources per tile).
+template <int K>
+__global__ void __launch_bounds__(kBlock) k_prk_out(const float *rank, uint64_t n, uint32_t k, float *out) {
+    __shared__ float t[32][K + 1];
+    for (uint64_t v0 = (uint64_t)blockIdx.x * 32; v0 < n; v0 += (uint64_t)gridDim.x * 32) {
+        for (int i = threadIdx.x; i < 32 * K; i += kBlock) {
+            int vv = i / K, s = i % K;
+            if (v0 + vv < n) t[vv][s] = rank[(v0 + vv) * K + s];
+        }
+        __syncthreads();
+        for (int i = threadIdx.x; i < 32 * K; i += kBlock) {
+            int s = i / 32, vv = i % 32;
+            if ((uint32_t)s < k && v0 + vv < n) out[(uint64_t)s * n + v0 + vv] = t[vv][s];
+        }
+        __syncthreads();
+    }
+}
+
 // Bin construction, in two passes over contiguous vertex ranges (one per
 // CTA) so that each list keeps ascending row order.  counts[blk*4 + t]:
 // rows of `mid`, rows of `big`, rows of `longs`, chunk items.
@@ -454,7 +663,92 @@ void pagerank_impl(ptg_graph *g, bool personalized, uint32_t src, double damping
     rr.iterations = iters;
 }
 
+template <class OffT, int K>
+void ppr_multi_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, float *d_rows, double damping,
+                    uint32_t iters, RunResult &rr) {
+    ptg_ctx *ctx = g->ctx;
+    Workspace &ws = ctx->ws;
+    cudaStream_t st = ctx->stream;
+    const uint64_t n = g->n;
+    const int sms = ctx->sm_count;
+    if (!g->pr_bins_built) build_pr_bins<OffT>(g);
+    ws.aux.ensure(std::max<uint64_t>(g->n_pr_items, 1) * K * 8);  // chunk partials
+    ws.aux2.ensure(2 * n * K * 4 + 64);                          // values ping-pong
+    ws.bsum.ensure(1024 * 8);
+    float *c[2] = {ws.aux2.as<float>(), ws.aux2.as<float>() + n * K};
+    double *dang = ws.bsum.as<double>();                            // [2][K]
+    uint32_t *d_src = reinterpret_cast<uint32_t *>(dang + 2 * K);  // [K]
+    uint32_t lanes[K];
+    for (int s = 0; s < K; s++) lanes[s] = (uint32_t)s < k ? h_srcs[s] : 0xFFFFFFFFu;
+    PTG_CUDA_TRY(cudaMemcpyAsync(d_src, lanes, sizeof(lanes), cudaMemcpyHostToDevice, st));
+    PTG_CUDA_TRY(cudaMemsetAsync(c[0], 0, n * K * 4, st));
+    const OffT *off = g->d_off.as<OffT>();
+    launch(ctx, "k_prk_init", k_prk_init<OffT, K>, 1, 32, 0, st, off, (const uint32_t *)d_src, c[0], dang);
+    PrBins bins;
+    bins.mid = g->d_pr_mid.as<uint32_t>();
+    bins.n_mid = g->n_pr_mid;
+    bins.big = g->d_pr_big.as<uint32_t>();
+    bins.n_big = g->n_pr_big;
+    bins.items = g->d_pr_items.as<uint2>();
+    bins.n_items = g->n_pr_items;
+    bins.longs = g->d_pr_longs.as<uint2>();
+    bins.n_longs = g->n_pr_longs;
+    bins.partial = ws.aux.as<float2>();
+    int fill_grid = grid_for(n, kBlock, sms * 8);
+    for (uint32_t it = 0; it < iters; it++) {
+        int cin = it & 1, cout = cin ^ 1;
+        PTG_CUDA_TRY(cudaMemsetAsync(dang + cout * K, 0, K * 8, st));
+        MsArgs a;
+        a.n = n;
+        a.off = off;
+        a.col = g->d_col.as<uint32_t>();
+        a.cin = c[cin];
+        a.cout = c[cout];
+        a.dang_in = dang + cin * K;
+        a.dang_out = dang + cout * K;
+        a.src = d_src;
+        a.d = damping;
+        a.last = it + 1 == iters;
+        launch(ctx, "k_prk_small", k_prk_small<OffT, K>, fill_grid, kBlock, 0, st, a);
+        if (bins.n_mid)
+            launch(ctx, "k_prk_mid", k_prk_mid<OffT, K>, grid_for(bins.n_mid * 8, kBlock, sms * 8), kBlock, 0, st, a,
+                   bins);
+        if (bins.n_big)
+            launch(ctx, "k_prk_big", k_prk_big<OffT, K>, grid_for(bins.n_big * 32, kBlock, sms * 8), kBlock, 0, st, a,
+                   bins);
+        if (bins.n_items) {
+            launch(ctx, "k_prk_chunks", k_prk_chunks<OffT, K>, grid_for(bins.n_items * 32, kBlock, sms * 8), kBlock,
+                   0, st, a, bins);
+            launch(ctx, "k_prk_long", k_prk_long<OffT, K>, grid_for(bins.n_longs, kBlock, sms * 2), kBlock, 0, st, a,
+                   bins);
+        }
+        PTG_CUDA_TRY(cudaGetLastError());
+        rr.edges_relaxed += g->m;
+    }
+    launch(ctx, "k_prk_out", k_prk_out<K>, grid_for((n + 31) / 32, 1, sms * 8), kBlock, 0, st,
+           (const float *)c[iters & 1], n, k, d_rows);
+    PTG_CUDA_TRY(cudaGetLastError());
+    rr.iterations += iters;
+}
+
 }  // namespace
+
+// Personalized PageRank of k <= 8 sources in one pass (4- or 8-wide values);
+// each row of d_rows equals run_pagerank(personalized, that source) bit for bit.
+void run_ppr_multi(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, float *d_rows, double damping, uint32_t iters,
+                   RunResult &rr) {
+    PTG_REQUIRE(!g->out_of_core, PTG_ERR_UNSUPPORTED, "PageRank needs the graph resident in HBM");
+    PTG_REQUIRE(g->symmetric, PTG_ERR_UNSUPPORTED, "pull PageRank needs a symmetric CSR (PTG_CSR_SYMMETRIC)");
+    PTG_REQUIRE(k >= 1 && k <= 8, PTG_ERR_INVALID, "a multi-source PageRank pass holds 1..8 sources");
+    PTG_REQUIRE(iters >= 1, PTG_ERR_INVALID, "PageRank needs at least one iteration");
+    if (g->off64) {
+        if (k <= 4) ppr_multi_impl<unsigned long long, 4>(g, h_srcs, k, d_rows, damping, iters, rr);
+        else ppr_multi_impl<unsigned long long, 8>(g, h_srcs, k, d_rows, damping, iters, rr);
+    } else {
+        if (k <= 4) ppr_multi_impl<uint32_t, 4>(g, h_srcs, k, d_rows, damping, iters, rr);
+        else ppr_multi_impl<uint32_t, 8>(g, h_srcs, k, d_rows, damping, iters, rr);
+    }
+}
 
 // Degree bins of a resident graph, built now rather than on first use.
 void pr_prepare_graph(ptg_graph *g) {

@@ -254,9 +254,6 @@ struct ptg_graph {
     ptg::DevBuf d_pr_mid, d_pr_big, d_pr_items, d_pr_longs;  // PageRank rows binned by degree
     uint64_t n_pr_mid = 0, n_pr_big = 0, n_pr_items = 0, n_pr_longs = 0;
     bool pr_bins_built = false;
-    ptg::DevBuf d_ppr_items, d_ppr_longs;  // long-row chunks (multi-source PPR)
-    uint64_t n_ppr_items = 0, n_ppr_longs = 0;
-    bool ppr_items_built = false;
     // out-of-core
     bool out_of_core = false;
     uint64_t resident_edges = 0;

@@ -43,7 +43,6 @@ bool ms_group(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_rows
 uint32_t ms_group_size(bool weighted);
 void ms_prepare_graph(ptg_graph *g);
 uint32_t ppr_group_size();
-void ppr_prepare_graph(ptg_graph *g);
 void run_ppr_group(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, float *d_rows, double damping,
                    uint32_t iters, RunResult &rr);
 void trav_prepare_graph(ptg_graph *g);
@@ -59,11 +58,11 @@ struct Entry {
     bool owned = false;
     bool busy = false;                 // out-of-core graphs: one query at a time
     std::vector<ptg_graph *> views;    // per lane (resident graphs)
-    // cost per kind (ms) of one single-source query, of one fused pass of up
-    // to 64 sources and of a full-width pass; measured once with the device
-    // otherwise idle when the graph is registered (calibrated), else moving
-    // averages of served batches; negative until known
-    double single_ms[3] = {-1, -1, -1}, fused64_ms[3] = {-1, -1, -1}, fused_ms[3] = {-1, -1, -1};
+    // cost per kind (ms) of one single-source query, of one narrow fused pass
+    // (up to small_k(kind) sources) and of a full-width pass; measured once
+    // with the device otherwise idle when the graph is registered
+    // (calibrated), else moving averages of served batches; negative until known
+    double single_ms[3] = {-1, -1, -1}, fused_small_ms[3] = {-1, -1, -1}, fused_ms[3] = {-1, -1, -1};
     bool calibrated = false;
 };
 
@@ -126,13 +125,8 @@ ptg_graph *make_view(ptg_graph *g, ptg_ctx *lane) {
     alias(v->d_pr_longs, g->d_pr_longs);
     alias(v->d_nzbm, g->d_nzbm);
     alias(v->d_pull_items, g->d_pull_items);
-    alias(v->d_ppr_items, g->d_ppr_items);
-    alias(v->d_ppr_longs, g->d_ppr_longs);
     v->n_pull_items = g->n_pull_items;
     v->pull_items_built = g->pull_items_built;
-    v->n_ppr_items = g->n_ppr_items;
-    v->n_ppr_longs = g->n_ppr_longs;
-    v->ppr_items_built = g->ppr_items_built;
     v->n_pr_mid = g->n_pr_mid;
     v->n_pr_big = g->n_pr_big;
     v->n_pr_items = g->n_pr_items;
@@ -161,8 +155,6 @@ void drop_view(ptg_graph *v, const ptg_graph *g) {
     detach(v->d_pr_longs, g->d_pr_longs);
     detach(v->d_nzbm, g->d_nzbm);
     detach(v->d_pull_items, g->d_pull_items);
-    detach(v->d_ppr_items, g->d_ppr_items);
-    detach(v->d_ppr_longs, g->d_ppr_longs);
     delete v;
 }
 
@@ -184,6 +176,10 @@ struct ptg_server {
 };
 
 namespace {
+
+// Batch size up to which a fused pass runs narrow: one mask word for BFS
+// (64 sources), the 64-lane pass for SSSP, an 8-lane group for PPR.
+uint32_t small_k(uint32_t kind) { return kind == PTG_Q_PPR ? 8u : 64u; }
 
 uint32_t kind_max(const ptg_server *s, uint32_t kind) {
     uint32_t k = kind == PTG_Q_BFS ? ms_group_size(false) : kind == PTG_Q_SSSP ? ms_group_size(true)
@@ -228,7 +224,8 @@ bool take_batch(ptg_server *s, Batch &b) {
     if (e.g->out_of_core || k == 1) b.fused = false;
     else if (e.single_ms[kd] < 0) b.fused = false;
     else if (e.fused_ms[kd] < 0) b.fused = true;
-    else b.fused = (k <= 64 && e.fused64_ms[kd] > 0 ? e.fused64_ms[kd] : e.fused_ms[kd]) < k * e.single_ms[kd];
+    else b.fused = (k <= small_k(kd) && e.fused_small_ms[kd] > 0 ? e.fused_small_ms[kd] : e.fused_ms[kd]) <
+                   k * e.single_ms[kd];
     if (!b.fused) k = 1;
     b.ent = &e;
     b.graph = best->first.first;
@@ -347,7 +344,7 @@ void lane_loop(ptg_server *s, size_t li) {
     }
 }
 
-// Times one single-source query and fused passes of 64 and of the full width
+// Times one single-source query, a narrow fused pass and a full-width one
 // for every kind the graph serves, on lane 0 (sources: non-isolated vertices
 // spread over the first 2^20 ids).  Results go to one device scratch row.
 template <class OffT>
@@ -391,13 +388,13 @@ void calibrate(ptg_server *s, uint32_t gid) {
     for (uint32_t kind = 0; kind < 3; kind++) {
         if (kind == PTG_Q_SSSP && !g->weighted) continue;
         if (kind == PTG_Q_PPR && !g->symmetric) continue;
-        uint32_t kmax = kind_max(s, kind);
+        uint32_t kmax = kind_max(s, kind), ks = std::min(small_k(kind), kmax);
         double sm = run(kind, 1, false);
-        double f64 = kmax > 1 ? run(kind, std::min<uint32_t>(64, kmax), true) : -1;
-        double fm = kmax > 64 ? run(kind, kmax, true) : f64;
+        double fs = kmax > 1 ? run(kind, ks, true) : -1;
+        double fm = kmax > ks ? run(kind, kmax, true) : fs;
         std::lock_guard<std::mutex> lk(s->mu);
         e.single_ms[kind] = sm;
-        e.fused64_ms[kind] = f64;
+        e.fused_small_ms[kind] = fs;
         e.fused_ms[kind] = fm;
     }
     std::lock_guard<std::mutex> lk(s->mu);
@@ -418,7 +415,6 @@ ptg_status register_entry(ptg_server *s, ptg_graph *g, bool owned, uint32_t *gra
                 if (g->symmetric) {
                     pr_prepare_graph(g);
                     ms_prepare_graph(g);
-                    ppr_prepare_graph(g);
                 }
                 PTG_CUDA_TRY(cudaStreamSynchronize(g->ctx->stream));
             });
