@@ -121,14 +121,18 @@ __device__ __forceinline__ void relax_probe(const PushTargets &t, uint32_t v, ui
 }
 
 // Build the frontier queue from its bitmap (a warp per 32 words, one atomic
-// per warp for its place in the queue), fold the frontier into the visited
+// per CTA step for the CTA's place in the queue: a per-warp atomic on the one
+// tail counter serialised dense levels), fold the frontier into the visited
 // bitmap (BFS) and take near vertices out of the far pile (SSSP).
 __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t *bm, uint64_t words, uint32_t *q,
                                                     TravCtl *ctl, uint32_t *vis, uint32_t *far_bm) {
-    const unsigned lane = lane_id();
-    uint64_t nwarps = (uint64_t)gridDim.x * (kBlock / 32);
-    for (uint64_t c = (uint64_t)blockIdx.x * (kBlock / 32) + (threadIdx.x >> 5); c * 32 < words; c += nwarps) {
-        uint64_t wd = c * 32 + lane;
+    constexpr int kWarps = kBlock / 32;
+    __shared__ uint32_t s_warp[kWarps];
+    __shared__ uint32_t s_base;
+    const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+    const uint64_t step = (uint64_t)gridDim.x * kWarps;
+    for (uint64_t c0 = (uint64_t)blockIdx.x * kWarps; c0 * 32 < words; c0 += step) {
+        uint64_t wd = (c0 + wid) * 32 + lane;
         uint32_t word = wd < words ? bm[wd] : 0u;
         if (word) {
             if (vis) vis[wd] |= word;
@@ -140,11 +144,20 @@ __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t *bm, uint64_t
             uint32_t y = __shfl_up_sync(0xffffffffu, pre, o);
             if (lane >= (unsigned)o) pre += y;
         }
-        uint32_t total = __shfl_sync(0xffffffffu, pre, 31);
-        uint32_t base = 0;
-        if (lane == 31 && total) base = atomicAdd(&ctl->next_tail, total);
-        base = __shfl_sync(0xffffffffu, base, 31);
-        uint32_t pos = base + pre - cnt;
+        if (lane == 31) s_warp[wid] = pre;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t run = 0;
+            for (int w = 0; w < kWarps; w++) {
+                uint32_t t = s_warp[w];
+                s_warp[w] = run;
+                run += t;
+            }
+            s_base = run ? atomicAdd(&ctl->next_tail, run) : 0u;
+        }
+        __syncthreads();
+        uint32_t pos = s_base + s_warp[wid] + pre - cnt;
+        __syncthreads();  // s_warp / s_base are rewritten by the next step
         while (word) {
             int b = __ffs(word) - 1;
             word &= word - 1;
