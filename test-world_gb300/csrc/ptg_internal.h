@@ -115,6 +115,7 @@ struct TravCtl {
     unsigned long long edges_done;// running total of edges expanded (stats)
     unsigned long long m_unvisited; // BFS direction heuristic
     unsigned long long far_min;   // min dist over the far pile (near/far SSSP)
+    unsigned long long next_E;    // edges of the next frontier (summed by k_compact for BFS)
     unsigned int F;               // current frontier size
     unsigned int next_tail;       // next frontier append cursor
     unsigned int far_count;       // far pile size

@@ -123,9 +123,14 @@ __device__ __forceinline__ void relax_probe(const PushTargets &t, uint32_t v, ui
 // Build the frontier queue from its bitmap (a warp per 32 words, one atomic
 // per CTA step for the CTA's place in the queue: a per-warp atomic on the one
 // tail counter serialised dense levels), fold the frontier into the visited
-// bitmap (BFS) and take near vertices out of the far pile (SSSP).
+// bitmap (BFS) and take near vertices out of the far pile (SSSP).  With off
+// given it also sums the new frontier's degrees into ctl->next_E, which the
+// host reads with the frontier size and uses for the next push/pull choice.
+template <class OffT>
 __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t *bm, uint64_t words, uint32_t *q,
-                                                    TravCtl *ctl, uint32_t *vis, uint32_t *far_bm) {
+                                                    TravCtl *ctl, uint32_t *vis, uint32_t *far_bm,
+                                                    const OffT *off) {
+    unsigned long long degsum = 0;
     constexpr int kWarps = kBlock / 32;
     __shared__ uint32_t s_warp[kWarps];
     __shared__ uint32_t s_base;
@@ -161,8 +166,14 @@ __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t *bm, uint64_t
         while (word) {
             int b = __ffs(word) - 1;
             word &= word - 1;
-            q[pos++] = (uint32_t)(wd * 32 + b);
+            uint32_t v = (uint32_t)(wd * 32 + b);
+            q[pos++] = v;
+            if (off) degsum += (unsigned long long)(off[v + 1] - off[v]);
         }
+    }
+    if (off) {
+        degsum = block_reduce_sum(degsum);
+        if (threadIdx.x == 0 && degsum) atomicAdd(&ctl->next_E, degsum);
     }
 }
 
@@ -643,6 +654,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
     if (allow_bu) build_nonzero_bits<OffT>(g);
     int cur = 0;
     uint64_t F = init.F, m_unvisited = g->m;
+    uint64_t next_E = 0;  // edges of the frontier (BFS direction choice); the seed level runs top-down
     bool far_nonempty = false;
     const int compact_grid = grid_for((words + 31) / 32, kBlock / 32, sms * 8);
     uint32_t threshold = init.threshold, level_val = base;
@@ -680,8 +692,9 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
             launch(ctx, "k_far_split", k_far_split, grid_for(words, kBlock, sms * 8), kBlock, 0, st,
                    ws.farbm.as<uint32_t>(), words, (const uint32_t *)d_value, ws.bm[cur].as<uint32_t>(),
                    (const TravCtl *)d_ctl);
-            launch(ctx, "k_compact", k_compact, compact_grid, kBlock, 0, st, (const uint32_t *)ws.bm[cur].as<uint32_t>(),
-                   words, ws.q[cur].as<uint32_t>(), d_ctl, (uint32_t *)nullptr, (uint32_t *)nullptr);
+            launch(ctx, "k_compact", k_compact<OffT>, compact_grid, kBlock, 0, st,
+                   (const uint32_t *)ws.bm[cur].as<uint32_t>(), words, ws.q[cur].as<uint32_t>(), d_ctl,
+                   (uint32_t *)nullptr, (uint32_t *)nullptr, (const OffT *)nullptr);
             PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
             PTG_CUDA_TRY(cudaStreamSynchronize(st));
             F = h_ctl->next_tail;
@@ -712,18 +725,15 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         }
         uint64_t E = 0;
         if (allow_bu) {
-            PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
-            PTG_CUDA_TRY(cudaStreamSynchronize(st));
-            E = h_ctl->E;
+            // the frontier's edge count came with its size (k_compact), so
+            // the push/pull choice needs no round trip of its own
+            E = next_E;
             if (!bottom_up && (double)E > (double)m_unvisited / alpha) bottom_up = true;
             else if (bottom_up && (double)F < (double)n / beta) bottom_up = false;
             m_unvisited = m_unvisited > E ? m_unvisited - E : 0;
         }
         if (bottom_up) {
             rr.bottom_up_rounds++;
-            if (h_ctl->level_val != level_val) {
-                PTG_CUDA_TRY(cudaMemcpyAsync(&d_ctl->level_val, &level_val, 4, cudaMemcpyHostToDevice, st));
-            }
             launch(ctx, "k_bottom_up", k_bottom_up<OffT>, grid_for((words + kBuWords - 1) / kBuWords, kBuWarps, sms * 8),
                    kBlock, 0, st, n, off, col, bm_cur, (const uint32_t *)g->d_nzbm.as<uint32_t>(), pt);
         } else {
@@ -838,8 +848,9 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
             }
         }
         // next frontier: queue from the bitmap
-        launch(ctx, "k_compact", k_compact, compact_grid, kBlock, 0, st, (const uint32_t *)bm_nxt, words, q_nxt,
-               d_ctl, vis, use_far ? ws.farbm.as<uint32_t>() : (uint32_t *)nullptr);
+        launch(ctx, "k_compact", k_compact<OffT>, compact_grid, kBlock, 0, st, (const uint32_t *)bm_nxt, words, q_nxt,
+               d_ctl, vis, use_far ? ws.farbm.as<uint32_t>() : (uint32_t *)nullptr,
+               allow_bu ? off : (const OffT *)nullptr);
         PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
         PTG_CUDA_TRY(cudaStreamSynchronize(st));
         PTG_REQUIRE(h_ctl->error == 0, PTG_ERR_CUDA, "frontier overflow in relax");
@@ -852,10 +863,12 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
             link_open = false;
         }
         F = h_ctl->next_tail;
+        next_E = h_ctl->next_E;
         if (use_far) far_nonempty = true;
         TravCtl upd = *h_ctl;
         upd.F = (uint32_t)F;
         upd.next_tail = 0;
+        upd.next_E = 0;
         upd.bu_next = 0;
         level_val++;
         upd.level_val = level_val;
