@@ -335,3 +335,24 @@ def test_hub_placement(ptg, ctx, oracle):
     assert sh["partitions_cached"] > 0 and sh["link_bytes"] < sn["link_bytes"]
     assert (G.bfs(0) == oracle.bfs(off, col, 0, method="queue")).all()
     assert (G.cc() == oracle.cc(off, col)).all()
+
+
+def test_mssssp_distances_beyond_16_bits(ptg, ctx, oracle):
+    """Multi-source SSSP runs with 16-bit distances when they fit; a graph whose
+    distances pass 65534 reruns the group at 32 bits with the same results."""
+    rng = np.random.default_rng(3)
+    n = 3000
+    edges = [(i, i + 1) for i in range(n - 1)] + list(map(tuple, rng.integers(0, n, (4000, 2))))
+    off, col = _sym_csr(n, edges)
+    w = np.empty(col.size, np.uint32)
+    for v in range(n):  # symmetric weights from the unordered pair
+        for e in range(int(off[v]), int(off[v + 1])):
+            a, b = min(v, int(col[e])), max(v, int(col[e]))
+            w[e] = 20000 + (a * 131 + b * 7) % 30000
+    G = ctx.graph(off, col, w, symmetric=True)
+    srcs = np.array([0, 1, 1500, 2999], np.uint32)
+    ms = G.mssssp(srcs)
+    for i, s in enumerate(srcs):
+        ref = oracle.sssp(off, col, w, int(s))
+        assert ref[ref != 0xFFFFFFFF].max() > 65535
+        assert (ms[i] == ref).all()
