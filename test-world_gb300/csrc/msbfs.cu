@@ -320,17 +320,23 @@ __global__ void __launch_bounds__(kBlock) k_msb_pull_big(const uint2 *items, uin
 // ---------------------------------------------------------------------------
 // MS-SSSP (64 sources per group)
 // ---------------------------------------------------------------------------
+// Source i of a group lives in distance word i of each vertex; lane l handles
+// the adjacent words 2l and 2l+1, and its sources' bits in the 64-bit masks
+// are l and 32 + l (so a warp's two ballots form a mask directly).
+__device__ __forceinline__ u64 mss_bit(uint32_t i) { return 1ull << ((i & 1u) ? 32u + (i >> 1) : (i >> 1)); }
+
 __global__ void k_mss_seed(const uint32_t *srcs, uint32_t k, u64 *A, uint32_t *dist, uint32_t base) {
     for (uint32_t i = threadIdx.x; i < k; i += blockDim.x) {
         uint32_t s = srcs[i];
-        atomicOr(&A[s], 1ull << i);
+        atomicOr(&A[s], mss_bit(i));
         dist[(uint64_t)s * 64 + i] = base;
     }
 }
 
 // MS-SSSP round: a warp relaxes one edge at a time for all 64 sources (lane l:
-// sources l and l+32), four edges per step so eight distance loads per lane
-// are in flight.  Edge slots are tiled like the single-source expand.
+// sources 2l and 2l+1, one 8-byte load), four edges per step so four distance
+// loads per lane are in flight.  Edge slots are tiled like the single-source expand.  The
+// kernel is instruction-bound, so per-edge bookkeeping is done lane-parallel.
 template <class OffT>
 __global__ void __launch_bounds__(kBlock) k_mss_relax(const uint32_t *q, const OffT *sc, const OffT *rs,
                                                       const uint32_t *tr, const uint32_t *col, const uint32_t *w,
@@ -368,46 +374,70 @@ __global__ void __launch_bounds__(kBlock) k_mss_relax(const uint32_t *q, const O
                 delta = rsv - scv;
                 u = staged ? s_u[r] : q[r];
             };
-            uint64_t next;
-            OffT delta;
-            uint32_t u;
-            row_info(row, next, delta, u);
-            u64 am = A[u];
-            uint32_t du0 = dist[(uint64_t)u * 64 + lane], du1 = dist[(uint64_t)u * 64 + 32 + lane];
-            for (uint64_t j = w0; j < w1; j += 4) {
-                uint32_t vv[4], ww[4], cur0[4], cur1[4], nd0[4], nd1[4];
+            // Edges go 32 at a time: lane b finds the row of edge b and loads
+            // its target and weight once; the warp then walks the 32 edges
+            // taking them from the lanes with shuffles (the row bookkeeping
+            // is done once per edge, not once per edge and lane).
+            uint32_t cur_u = 0xFFFFFFFFu;
+            u64 am = 0;
+            uint32_t du0 = 0, du1 = 0;
+            for (uint64_t j = w0; j < w1; j += 32) {
+                uint64_t jj = j + lane;
+                bool ok = jj < w1;
+                uint64_t r = row, nx;
+                OffT delta;
+                uint32_t ul;
+                row_info(r, nx, delta, ul);
+                while (ok && jj >= nx) {
+                    r++;
+                    row_info(r, nx, delta, ul);
+                }
+                uint32_t vl = 0, wl = 0;
+                if (ok) {
+                    uint64_t e = (uint64_t)(OffT)(delta + (OffT)jj);
+                    vl = __ldcs(col + e);
+                    wl = __ldcs(w + e);
+                }
+                row = __shfl_sync(0xffffffffu, r, 31);
+                const uint32_t cnt = (uint32_t)min((uint64_t)32, w1 - j);
+                for (uint32_t b = 0; b < cnt; b += 4) {
+                    uint32_t vv[4], nd0[4], nd1[4], cur0[4], cur1[4];
 #pragma unroll
-                for (int b = 0; b < 4; b++) {
-                    uint64_t jj = j + b;
-                    vv[b] = 0;
-                    nd0[b] = nd1[b] = PTG_UNREACHED;
-                    if (jj < w1) {
-                        while (jj >= next) {
-                            row++;
-                            row_info(row, next, delta, u);
-                            am = A[u];
-                            du0 = dist[(uint64_t)u * 64 + lane];
-                            du1 = dist[(uint64_t)u * 64 + 32 + lane];
+                    for (int t = 0; t < 4; t++) {
+                        uint32_t src = (b + t) & 31u;
+                        uint32_t ut = __shfl_sync(0xffffffffu, ul, src);
+                        uint32_t wt = __shfl_sync(0xffffffffu, wl, src);
+                        vv[t] = __shfl_sync(0xffffffffu, vl, src);
+                        nd0[t] = nd1[t] = PTG_UNREACHED;
+                        if (b + t < cnt) {
+                            if (ut != cur_u) {  // warp-uniform: a new tail vertex
+                                cur_u = ut;
+                                am = A[ut];
+                                uint2 d = reinterpret_cast<const uint2 *>(dist + (uint64_t)ut * 64)[lane];
+                                du0 = d.x;
+                                du1 = d.y;
+                            }
+                            if ((am >> lane) & 1ull) nd0[t] = du0 + wt;
+                            if ((am >> (32 + lane)) & 1ull) nd1[t] = du1 + wt;
                         }
-                        uint64_t e = (uint64_t)(OffT)(delta + (OffT)jj);
-                        vv[b] = __ldcs(col + e);
-                        ww[b] = __ldcs(w + e);
-                        if ((am >> lane) & 1ull) nd0[b] = du0 + ww[b];
-                        if ((am >> (32 + lane)) & 1ull) nd1[b] = du1 + ww[b];
                     }
-                }
 #pragma unroll
-                for (int b = 0; b < 4; b++) {
-                    cur0[b] = nd0[b] != PTG_UNREACHED ? dist[(uint64_t)vv[b] * 64 + lane] : 0u;
-                    cur1[b] = nd1[b] != PTG_UNREACHED ? dist[(uint64_t)vv[b] * 64 + 32 + lane] : 0u;
-                }
+                    for (int t = 0; t < 4; t++) {
+                        cur0[t] = cur1[t] = 0u;
+                        if ((nd0[t] & nd1[t]) != PTG_UNREACHED) {
+                            uint2 c = reinterpret_cast<const uint2 *>(dist + (uint64_t)vv[t] * 64)[lane];
+                            cur0[t] = c.x;
+                            cur1[t] = c.y;
+                        }
+                    }
 #pragma unroll
-                for (int b = 0; b < 4; b++) {
-                    bool i0 = nd0[b] < cur0[b], i1 = nd1[b] < cur1[b];
-                    if (i0) atomicMin(&dist[(uint64_t)vv[b] * 64 + lane], nd0[b]);
-                    if (i1) atomicMin(&dist[(uint64_t)vv[b] * 64 + 32 + lane], nd1[b]);
-                    unsigned b0 = __ballot_sync(0xffffffffu, i0), b1 = __ballot_sync(0xffffffffu, i1);
-                    if (lane == 0 && (b0 | b1)) atomicOr(&N[vv[b]], (u64)b0 | ((u64)b1 << 32));
+                    for (int t = 0; t < 4; t++) {
+                        bool i0 = nd0[t] < cur0[t], i1 = nd1[t] < cur1[t];
+                        if (i0) atomicMin(&dist[(uint64_t)vv[t] * 64 + 2 * lane], nd0[t]);
+                        if (i1) atomicMin(&dist[(uint64_t)vv[t] * 64 + 2 * lane + 1], nd1[t]);
+                        unsigned b0 = __ballot_sync(0xffffffffu, i0), b1 = __ballot_sync(0xffffffffu, i1);
+                        if (lane == 0 && (b0 | b1)) atomicOr(&N[vv[t]], (u64)b0 | ((u64)b1 << 32));
+                    }
                 }
             }
         }
