@@ -334,8 +334,8 @@ __global__ void k_mss_seed(const uint32_t *srcs, uint32_t k, u64 *A, uint32_t *d
 }
 
 // MS-SSSP round: a warp relaxes one edge at a time for all 64 sources (lane l:
-// sources 2l and 2l+1, one 8-byte load), four edges per step so four distance
-// loads per lane are in flight.  Edge slots are tiled like the single-source expand.  The
+// sources 2l and 2l+1, one 8-byte load), eight edges per step so eight
+// distance loads per lane are in flight.  Edge slots are tiled like the single-source expand.  The
 // kernel is instruction-bound, so per-edge bookkeeping is done lane-parallel.
 template <class OffT>
 __global__ void __launch_bounds__(kBlock) k_mss_relax(const uint32_t *q, const OffT *sc, const OffT *rs,
@@ -400,10 +400,10 @@ __global__ void __launch_bounds__(kBlock) k_mss_relax(const uint32_t *q, const O
                 }
                 row = __shfl_sync(0xffffffffu, r, 31);
                 const uint32_t cnt = (uint32_t)min((uint64_t)32, w1 - j);
-                for (uint32_t b = 0; b < cnt; b += 4) {
-                    uint32_t vv[4], nd0[4], nd1[4], cur0[4], cur1[4];
+                for (uint32_t b = 0; b < cnt; b += 8) {
+                    uint32_t vv[8], nd0[8], nd1[8], cur0[8], cur1[8];
 #pragma unroll
-                    for (int t = 0; t < 4; t++) {
+                    for (int t = 0; t < 8; t++) {
                         uint32_t src = (b + t) & 31u;
                         uint32_t ut = __shfl_sync(0xffffffffu, ul, src);
                         uint32_t wt = __shfl_sync(0xffffffffu, wl, src);
@@ -422,7 +422,7 @@ __global__ void __launch_bounds__(kBlock) k_mss_relax(const uint32_t *q, const O
                         }
                     }
 #pragma unroll
-                    for (int t = 0; t < 4; t++) {
+                    for (int t = 0; t < 8; t++) {
                         cur0[t] = cur1[t] = 0u;
                         if ((nd0[t] & nd1[t]) != PTG_UNREACHED) {
                             uint2 c = reinterpret_cast<const uint2 *>(dist + (uint64_t)vv[t] * 64)[lane];
@@ -431,7 +431,7 @@ __global__ void __launch_bounds__(kBlock) k_mss_relax(const uint32_t *q, const O
                         }
                     }
 #pragma unroll
-                    for (int t = 0; t < 4; t++) {
+                    for (int t = 0; t < 8; t++) {
                         bool i0 = nd0[t] < cur0[t], i1 = nd1[t] < cur1[t];
                         if (i0) atomicMin(&dist[(uint64_t)vv[t] * 64 + 2 * lane], nd0[t]);
                         if (i1) atomicMin(&dist[(uint64_t)vv[t] * 64 + 2 * lane + 1], nd1[t]);
