@@ -60,7 +60,7 @@ def parse():
     p.add_argument("--serve-uploads", type=int, default=16)
     p.add_argument("--serve-requests", type=int, default=4000)
     p.add_argument("--serve-rate", type=float, default=2000.0)
-    p.add_argument("--serve-lanes", type=int, default=4)
+    p.add_argument("--serve-lanes", type=int, default=2)
     p.add_argument("--plain-sample", type=int, default=240)
     p.add_argument("--er-graphs", type=int, default=4096)
     p.add_argument("--batch-sources", type=int, default=1024)
