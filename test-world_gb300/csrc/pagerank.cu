@@ -1,4 +1,4 @@
-// pagerank.cu - pull PageRank and personalized PageRank as merge-path SpMV.
+// pagerank.cu - pull PageRank and personalized PageRank as degree-binned SpMV.
 //
 // The reference has no PageRank: prCaculateInShare (ptGraph/main.cu:891-959)
 // runs frontier bookkeeping with its kernel call commented out (937) and

@@ -8,7 +8,7 @@
 // every resident graph (same device arrays, the lane's stream).  Whenever a
 // lane is free it takes the group (graph, kind) whose oldest request is the
 // oldest queued overall, removes up to a batch of that group's requests and
-// runs them as one fused multi-source pass (msbfs.cu / pprbatch.cu), or as
+// runs them as one fused multi-source pass (msbfs.cu, pagerank.cu), or as
 // single-source queries in turn when the costs measured so far for that
 // graph and kind say k singles are cheaper than one pass (small batches on a
 // large graph).  Requests arriving meanwhile wait for the next free lane, so
