@@ -598,7 +598,12 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
     ws.bsum.ensure(kScanBlocks * 8);
     ws.ctl.ensure(sizeof(TravCtl));
     ws.h_ctl.ensure(sizeof(TravCtl));
-    bool use_far = kind == TRAV_SSSP && !(flags & PTG_REFERENCE_SCHEDULE);
+    // Near/far buckets save edge work in HBM; a streamed graph is bound by the
+    // host link, where every round re-copies its active partitions, so it
+    // relaxes in label-correcting rounds unless a bucket width is asked for
+    // (RMAT-26 all streamed: 9 rounds and 55 GB over the link instead of 18
+    // rounds and 107 GB).
+    bool use_far = kind == TRAV_SSSP && !(flags & PTG_REFERENCE_SCHEDULE) && (!g->out_of_core || delta != 0);
     if (use_far) ws.farbm.ensure(words * 4);
     TravCtl *d_ctl = ws.ctl.as<TravCtl>();
     TravCtl *h_ctl = ws.h_ctl.as<TravCtl>();
