@@ -420,6 +420,18 @@ __global__ void k_mark_partitions(const uint32_t *q, const TravCtl *ctl, const O
     }
 }
 
+// A source vertex is active in a streamed partition if it is in this
+// level's frontier or, for SSSP and label propagation (which converge under
+// any order), if it improved earlier in this level: partitions streamed later
+// in a level then see the improvements of earlier ones (Gauss-Seidel order),
+// so fewer levels, and fewer re-copies, are needed.  Such a vertex stays in
+// the next frontier as well.  BFS keeps level-synchronous order (a vertex
+// found in this level must not pass on this level's value).
+template <int MODE>
+__device__ __forceinline__ bool part_active(const uint32_t *bm_cur, const PushTargets &t, uint32_t u) {
+    return bit_test(bm_cur, u) || (MODE != 0 && bit_test(t.bm_next, u));
+}
+
 // Out-of-core: relax every edge of one staged partition whose source vertex
 // is in the frontier bitmap.  Edge-centric tiles; the source row of each edge
 // is found by binary search over the tile's offsets (staged in shared memory).
@@ -445,7 +457,7 @@ __global__ void __launch_bounds__(kBlock) k_relax_partition(uint64_t e_begin, ui
             for (uint64_t k = threadIdx.x; k < nrows; k += kBlock) {
                 uint32_t u = (uint32_t)(r0 + k);
                 s_off[k] = off[u];
-                s_val[k] = bit_test(bm_cur, u) ? t.value[u] : PTG_UNREACHED;
+                s_val[k] = part_active<MODE>(bm_cur, t, u) ? t.value[u] : PTG_UNREACHED;
             }
             if (threadIdx.x == 0) s_off[nrows] = off[r0 + nrows];
         }
@@ -457,7 +469,7 @@ __global__ void __launch_bounds__(kBlock) k_relax_partition(uint64_t e_begin, ui
                 uval = s_val[row];
             } else {
                 uint64_t u = last_le(off, r0, r0 + nrows, j);
-                uval = bit_test(bm_cur, (uint32_t)u) ? t.value[u] : PTG_UNREACHED;
+                uval = part_active<MODE>(bm_cur, t, (uint32_t)u) ? t.value[u] : PTG_UNREACHED;
             }
             if (uval == PTG_UNREACHED) continue;
             uint64_t le = j - e_begin;
