@@ -61,6 +61,7 @@ def parse():
     p.add_argument("--serve-requests", type=int, default=4000)
     p.add_argument("--serve-rate", type=float, default=2000.0)
     p.add_argument("--serve-lanes", type=int, default=2)
+    p.add_argument("--serve-schedule", type=int, default=0, help="0: oldest first, 1: response ratio")
     p.add_argument("--plain-sample", type=int, default=240)
     p.add_argument("--er-graphs", type=int, default=4096)
     p.add_argument("--batch-sources", type=int, default=1024)
@@ -182,7 +183,7 @@ def serve_workload(args):
     gidx = rng.integers(0, len(graphs), N)
     srcs = np.array([nz[g][rng.integers(nz[g].size)] for g in gidx], dtype=np.uint32)
 
-    srv = ptgraph.Server(ctx, lanes=args.serve_lanes)
+    srv = ptgraph.Server(ctx, lanes=args.serve_lanes, schedule=args.serve_schedule)
     t0 = time.time()
     up = [srv.upload(off, col, w) for off, col, w in graphs]
     upload_s = time.time() - t0
@@ -249,7 +250,7 @@ def serve_workload(args):
                                                  "resident_graphs", "streamed_graphs", "budget_bytes",
                                                  "committed_bytes", "busy_ms", "fused_requests",
                                                  "single_requests", "fused_batches", "fused_ms", "single_ms")},
-           "lanes": args.serve_lanes, "graphs": {"resident_scale": args.serve_scale, "upload_scales": scales,
+           "lanes": args.serve_lanes, "schedule": ["oldest", "response_ratio"][args.serve_schedule], "graphs": {"resident_scale": args.serve_scale, "upload_scales": scales,
                                                  "admitted_resident": [bool(r) for _, r in up]},
            "gen_s": gen_s, "upload_s": upload_s}
     # plain: one query at a time, same requests, host outputs

@@ -316,7 +316,16 @@ typedef struct ptg_server_config {
     double ppr_damping;           /* 0 = 0.85                                          */
     uint64_t memory_budget_bytes; /* graphs + lane workspaces; 0 = free HBM at
                                      creation minus 10%                                */
+    uint32_t schedule;            /* PTG_SCHEDULE_*                                    */
+    uint32_t reserved;
 } ptg_server_config;
+
+enum {
+    PTG_SCHEDULE_OLDEST = 0,         /* next group: the one holding the oldest request
+                                        (default; most batching under overload)        */
+    PTG_SCHEDULE_RESPONSE_RATIO = 1  /* next group: highest (wait + service) / service of
+                                        its oldest request (lower median latency)      */
+};
 
 ptg_status ptg_server_create(ptg_ctx *ctx, const ptg_server_config *cfg, ptg_server **out);
 /* Pending requests complete with PTG_ERR_CANCELLED; running batches finish. */

@@ -102,7 +102,8 @@ class ServerConfig(ctypes.Structure):
     _fields_ = [("lanes", ctypes.c_uint32), ("max_slots", ctypes.c_uint32), ("max_batch", ctypes.c_uint32),
                 ("queue_capacity", ctypes.c_uint32), ("ppr_iterations", ctypes.c_uint32),
                 ("no_calibration", ctypes.c_uint32), ("ppr_damping", ctypes.c_double),
-                ("memory_budget_bytes", ctypes.c_uint64)]
+                ("memory_budget_bytes", ctypes.c_uint64), ("schedule", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32)]
 
 
 class ServerStats(ctypes.Structure):
@@ -442,9 +443,10 @@ class Server:
     lanes that batch requests of the same graph and kind into fused passes."""
 
     def __init__(self, ctx, lanes=0, max_slots=0, max_batch=0, queue_capacity=0, ppr_iterations=0,
-                 ppr_damping=0.0, memory_budget_bytes=0, calibrate=True):
+                 ppr_damping=0.0, memory_budget_bytes=0, calibrate=True, schedule=0):
         cfg = ServerConfig()
         cfg.no_calibration = 0 if calibrate else 1
+        cfg.schedule = schedule
         cfg.lanes, cfg.max_slots, cfg.max_batch = lanes, max_slots, max_batch
         cfg.queue_capacity, cfg.ppr_iterations, cfg.ppr_damping = queue_capacity, ppr_iterations, ppr_damping
         cfg.memory_budget_bytes = memory_budget_bytes
