@@ -39,6 +39,15 @@ FALLBACK_HBM_GBS = 6800.0
 PR_DRAM_BYTES_PER_ITEM = (670.733312e6 + 5.081856e6) / (4194304 + 128307638)
 
 
+def make_ctx(args, device):
+    """Engine context on `device`, with the --tuning file applied if given."""
+    import ptgraph
+    ctx = ptgraph.Ctx(device)
+    if getattr(args, "tuning", ""):
+        ctx.load_tuning(args.tuning)
+    return ctx
+
+
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -50,6 +59,9 @@ def parse():
     p.add_argument("--sssp-sources", type=int, default=4)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--tuning", default="",
+                   help="autotuner JSON (python -m ptgraph.tune) applied to every context; "
+                        "default: the library's built-in tuning")
     p.add_argument("--workload", default="suite", choices=["suite", "batch", "serve", "ooc"],
                    help="suite: the in-HBM suite on RMAT-24 (default); batch: 1024-source MS-BFS/MS-SSSP "
                         "on RMAT-22 and CC over a batch of ER graphs, each against one-at-a-time calls; "
@@ -75,7 +87,7 @@ def batch_workload(args):
     """Config 4: batched queries against the plain one-at-a-time path (same results checked)."""
     import torch
     import ptgraph
-    ctx = ptgraph.Ctx(int(os.environ.get("LOCAL_RANK", "0")))
+    ctx = make_ctx(args, int(os.environ.get("LOCAL_RANK", "0")))
     scale = 22 if args.scale == 24 else args.scale
     off, col, w = ptgraph.gen_rmat(scale, 16, 0.57, 0.19, 0.19, seed=4, symmetric=True, wmin=1, wmax=63)
     n, m = off.size - 1, col.size
@@ -168,7 +180,7 @@ def serve_workload(args):
     import ptgraph
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    ctx = ptgraph.Ctx(local)
+    ctx = make_ctx(args, local)
     rng = np.random.default_rng(2000)
     t0 = time.time()
     graphs = [ptgraph.gen_rmat(args.serve_scale, 16, 0.57, 0.19, 0.19, seed=5, symmetric=True, wmin=1, wmax=63)]
@@ -328,7 +340,7 @@ def ooc_workload(args):
     run against the measured pinned host->device rate, plus GTEPS of the search."""
     import ptgraph
     local = int(os.environ.get("LOCAL_RANK", "0"))
-    ctx = ptgraph.Ctx(local)
+    ctx = make_ctx(args, local)
     t0 = time.time()
     off, col, w = ptgraph.gen_rmat(args.ooc_scale, 16, 0.57, 0.19, 0.19, seed=3, symmetric=False, wmin=1, wmax=63)
     gen_s = time.time() - t0
@@ -385,7 +397,7 @@ def multi_dev(G, srcs, out, name, st):
 
 def profile_case(args):
     import ptgraph
-    ctx = ptgraph.Ctx(int(os.environ.get("LOCAL_RANK", "0")))
+    ctx = make_ctx(args, int(os.environ.get("LOCAL_RANK", "0")))
     off, col, w, deg, sources, _ = make_workload(args)
     G = ctx.graph(off.astype(np.uint32), col, w, symmetric=True)
     out = {}
@@ -538,7 +550,8 @@ def workload_config(args):
                                                                             args.sssp_sources),
             "scale": args.scale, "edge_factor": 16, "bfs_sources": args.sources,
             "sssp_sources": args.sssp_sources, "pagerank_iterations": 20,
-            "l2": "inputs larger than L2 (CSR ~4.4 GB vs 129 MB L2); no flush"}
+            "l2": "inputs larger than L2 (CSR ~4.4 GB vs 129 MB L2); no flush",
+            "tuning": os.path.basename(args.tuning) if args.tuning else "built-in"}
 
 
 def main():
@@ -562,7 +575,7 @@ def main():
     import torch
     import ptgraph
     torch.cuda.set_device(local)
-    ctx = ptgraph.Ctx(local)
+    ctx = make_ctx(args, local)
     off, col, w, deg, sources, gen_s = make_workload(args)
     n, m = off.size - 1, col.size
     off32 = off.astype(np.uint32)

@@ -122,7 +122,8 @@ enum {
 };
 
 typedef struct ptg_partition_config {
-    uint64_t partition_bytes;     /* edge bytes per streamed partition; 0 = 256 MiB   */
+    uint64_t partition_bytes;     /* edge bytes per streamed partition; 0 = the
+                                     context's tuning (256 MiB unless tuned)          */
     uint64_t device_budget_bytes; /* bytes of HBM for resident edges; 0 = use frac   */
     double device_frac;           /* fraction of free HBM for resident edges; 0 = 0.9 */
     uint32_t n_staging_buffers;   /* 2 or 3 (double/triple buffering); 0 = 2          */
@@ -201,6 +202,49 @@ uint64_t ptg_ctx_launch_count(const ptg_ctx *ctx);
 uint32_t ptg_ctx_profile_entries(const ptg_ctx *ctx);
 ptg_status ptg_ctx_profile_entry(const ptg_ctx *ctx, uint32_t i, const char **name,
                                  uint64_t *launches, double *total_ms);
+
+/* Engine tuning: the partition size, degree-bin thresholds and launch shapes
+ * the reference hard-codes (fragment_size main.cu:66, the memory fractions,
+ * 56x1024 grids, the hot threshold 3600 gpu_kernels.cu:479).  The autotuner
+ * (ptgraph.tune) sweeps them on the device and writes them as JSON; a
+ * context applies a set with ptg_ctx_set_tuning.  None of them changes a BFS
+ * level, SSSP distance or CC label.  pr_mid and pr_chunk change PageRank's
+ * summation order (results stay within the 1e-6 tolerance); batched PPR and
+ * single PPR on one graph always share them, so their rows stay identical.
+ * Degree bins and multi-source pull items are built with the values in force
+ * when a graph is created (or first used); the others apply per call. */
+#define PTG_TUNING_VERSION 1u
+typedef struct ptg_tuning {
+    uint32_t version;            /* PTG_TUNING_VERSION                                  */
+    float bfs_alpha;             /* BFS turns to pull when frontier edges exceed the
+                                    unvisited edges / bfs_alpha (default 15)             */
+    float bfs_beta;              /* ... and back to push when the frontier holds fewer
+                                    than n / bfs_beta vertices (default 18)              */
+    float sssp_delta_scale;      /* default SSSP bucket width = this x the mean edge
+                                    weight (default 0.5; 0: label-correcting rounds)     */
+    uint32_t expand_ctas_per_sm; /* push relax (k_expand) CTAs per SM, 1..32 (default 8) */
+    uint32_t pr_ctas_per_sm;     /* PageRank SpMV CTAs per SM, 1..32 (default 8)         */
+    uint32_t pr_mid;             /* PageRank rows of 5..pr_mid edges run 8 lanes per
+                                    row, longer ones a warp (default 64; 8..pr_chunk)    */
+    uint32_t pr_chunk;           /* rows over pr_chunk edges are cut into pr_chunk-edge
+                                    pieces (default 4096; 128..65536)                    */
+    uint32_t ms_pull_small;      /* multi-source pull: rows up to this many edges take
+                                    a thread, longer ones warps (default 32; 1..4096)    */
+    uint32_t ms_pull_chunk;      /* edges per warp item of a long row (default 1024;
+                                    32..65536, a multiple of 32)                         */
+    uint32_t reserved0[2];       /* zero; keeps partition_bytes at byte offset 48       */
+    uint64_t partition_bytes;    /* edge bytes per partition of an out-of-core graph
+                                    created without a partition size (default 256 MiB;
+                                    1 MiB..16 GiB)                                       */
+    uint32_t reserved[8];
+} ptg_tuning;
+
+/* Built-in values (what the autotuner measured best on a GB300). */
+void ptg_tuning_defaults(ptg_tuning *t);
+/* PTG_OK if every field is in range (host-only, no GPU needed). */
+ptg_status ptg_tuning_validate(const ptg_tuning *t);
+ptg_status ptg_ctx_set_tuning(ptg_ctx *ctx, const ptg_tuning *t);
+ptg_status ptg_ctx_get_tuning(const ptg_ctx *ctx, ptg_tuning *t);
 
 /* Upload a CSR.  Edges live in HBM when they fit the budget; otherwise the
  * first partitions stay resident and the rest stream from pinned host memory

@@ -209,7 +209,7 @@ const char *ptg_status_string(ptg_status s) {
 void ptg_partition_config_default(ptg_partition_config *cfg) {
     if (!cfg) return;
     std::memset(cfg, 0, sizeof(*cfg));
-    cfg->partition_bytes = 256ull << 20;
+    cfg->partition_bytes = 0;  // the context's tuned size (256 MiB for the host-only planner)
     cfg->device_budget_bytes = 0;
     cfg->device_frac = 0.9;
     cfg->n_staging_buffers = 2;
@@ -235,6 +235,56 @@ ptg_status ptg_plan_partitions(uint64_t n, uint64_t m, const uint64_t *offsets_n
     return PTG_OK;
 }
 
+void ptg_tuning_defaults(ptg_tuning *t) {
+    if (!t) return;
+    std::memset(t, 0, sizeof(*t));
+    t->version = PTG_TUNING_VERSION;
+    t->bfs_alpha = 15.f;
+    t->bfs_beta = 18.f;
+    t->sssp_delta_scale = 0.5f;
+    t->expand_ctas_per_sm = 8;
+    t->pr_ctas_per_sm = 8;
+    t->pr_mid = 64;
+    t->pr_chunk = 4096;
+    t->ms_pull_small = 32;
+    t->ms_pull_chunk = 1024;
+    t->partition_bytes = 256ull << 20;
+}
+
+ptg_status ptg_tuning_validate(const ptg_tuning *t) {
+    if (!t || t->version != PTG_TUNING_VERSION) return PTG_ERR_INVALID;
+    auto finite_in = [](float x, float lo, float hi) { return x == x && x >= lo && x <= hi; };
+    if (!finite_in(t->bfs_alpha, 0.01f, 1e6f) || !finite_in(t->bfs_beta, 0.01f, 1e6f)) return PTG_ERR_INVALID;
+    if (!finite_in(t->sssp_delta_scale, 0.f, 1e6f)) return PTG_ERR_INVALID;
+    if (t->expand_ctas_per_sm < 1 || t->expand_ctas_per_sm > 32) return PTG_ERR_INVALID;
+    if (t->pr_ctas_per_sm < 1 || t->pr_ctas_per_sm > 32) return PTG_ERR_INVALID;
+    if (t->pr_chunk < 128 || t->pr_chunk > 65536) return PTG_ERR_INVALID;
+    if (t->pr_mid < 8 || t->pr_mid > t->pr_chunk) return PTG_ERR_INVALID;
+    if (t->ms_pull_small < 1 || t->ms_pull_small > 4096) return PTG_ERR_INVALID;
+    if (t->ms_pull_chunk < 32 || t->ms_pull_chunk > 65536 || t->ms_pull_chunk % 32) return PTG_ERR_INVALID;
+    if (t->partition_bytes < (1ull << 20) || t->partition_bytes > (16ull << 30)) return PTG_ERR_INVALID;
+    return PTG_OK;
+}
+
+ptg_status ptg_ctx_set_tuning(ptg_ctx *ctx, const ptg_tuning *t) {
+    if (!ctx) return PTG_ERR_INVALID;
+    ptg_status s = ptg_tuning_validate(t);
+    if (s != PTG_OK) {
+        std::lock_guard<std::mutex> lk(ctx->mu);
+        ctx->last_error = "tuning: a field is out of range or the version is not PTG_TUNING_VERSION";
+        return s;
+    }
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->tuning = *t;
+    return PTG_OK;
+}
+
+ptg_status ptg_ctx_get_tuning(const ptg_ctx *ctx, ptg_tuning *t) {
+    if (!ctx || !t) return PTG_ERR_INVALID;
+    *t = ctx->tuning;
+    return PTG_OK;
+}
+
 ptg_status ptg_ctx_create(int device, ptg_ctx **out) {
     if (!out) return PTG_ERR_INVALID;
     *out = nullptr;
@@ -246,6 +296,7 @@ ptg_status ptg_ctx_create(int device, ptg_ctx **out) {
     if (device < 0 || device >= count) return PTG_ERR_INVALID;
     auto *ctx = new ptg_ctx();
     ctx->device = device;
+    ptg_tuning_defaults(&ctx->tuning);
     ptg_status s = guard(ctx, [&] {
         PTG_CUDA_TRY(cudaSetDevice(device));
         cudaDeviceProp prop;
@@ -360,6 +411,8 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
         ptg_partition_config cfg;
         ptg_partition_config_default(&cfg);
         if (cfg_in) cfg = *cfg_in;
+        // no partition size given: the context's tuned one
+        if (!cfg_in || cfg.partition_bytes == 0) cfg.partition_bytes = ctx->tuning.partition_bytes;
         if (cfg.n_staging_buffers < 2) cfg.n_staging_buffers = 2;
         if (cfg.n_staging_buffers > 3) cfg.n_staging_buffers = 3;
         uint64_t bpe = g->weighted ? 8 : 4;

@@ -190,22 +190,21 @@ __global__ void __launch_bounds__(kBlock) k_msb_update(uint64_t n, const OffT *o
 // some frontier mask this level), so its scan stops as soon as it holds all
 // live sources it has not seen; sources whose search died out (small
 // components) no longer keep hubs scanning.  Work is split by degree so that
-// no thread walks a long adjacency alone: vertices of degree <= kPullSmall
-// are one thread each (k_msb_pull_small); the adjacency of every other vertex
-// is cut into kPullChunk-edge work items, one warp each (k_msb_pull_big),
+// no thread walks a long adjacency alone: vertices of degree <= small (a
+// tuning value, 32 by default) are one thread each (k_msb_pull_small); the
+// adjacency of every other vertex is cut into chunk-edge work items (1024 by
+// default), one warp each (k_msb_pull_big),
 // whose partial masks meet in N through atomicOr.  A neighbour's W words are
 // one 32-byte sector for W = 4, read with 16-byte vector loads.
-constexpr uint32_t kPullSmall = 32;
-constexpr uint32_t kPullChunk = 1024;
-
-// Work items (vertex, chunk) of the vertices above kPullSmall; counted first
+// Work items (vertex, chunk) of the vertices above `small`; counted first
 // (items == nullptr), then written.  Item order is irrelevant.
 template <class OffT>
-__global__ void k_pull_items(uint64_t n, const OffT *off, uint2 *items, unsigned long long *count) {
+__global__ void k_pull_items(uint64_t n, const OffT *off, uint32_t small, uint32_t chunk, uint2 *items,
+                             unsigned long long *count) {
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
         uint64_t deg = (uint64_t)(off[v + 1] - off[v]);
-        if (deg <= kPullSmall) continue;
-        uint32_t c = (uint32_t)((deg + kPullChunk - 1) / kPullChunk);
+        if (deg <= small) continue;
+        uint32_t c = (uint32_t)((deg + chunk - 1) / chunk);
         unsigned long long base = atomicAdd(count, (unsigned long long)c);
         if (items)
             for (uint32_t i = 0; i < c; i++) items[base + i] = make_uint2((uint32_t)v, i);
@@ -215,13 +214,13 @@ __global__ void k_pull_items(uint64_t n, const OffT *off, uint2 *items, unsigned
 template <class OffT, int W>
 __global__ void __launch_bounds__(kBlock) k_msb_pull_small(uint64_t n, const OffT *off, const uint32_t *col,
                                                            const u64 *F, const u64 *S, u64 *N,
-                                                           const u64 *live_in) {
+                                                           const u64 *live_in, uint32_t small) {
     u64 live[W];
 #pragma unroll
     for (int w = 0; w < W; w++) live[w] = live_in[w];
     for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
         OffT b = off[v], e = off[v + 1];
-        if (b == e || (uint64_t)(e - b) > kPullSmall) continue;
+        if (b == e || (uint64_t)(e - b) > small) continue;
         u64 s[W], need[W];
         load_mask<W>(S + v * W, s);
         bool none = true;
@@ -257,7 +256,7 @@ __global__ void __launch_bounds__(kBlock) k_msb_pull_small(uint64_t n, const Off
 template <class OffT, int W>
 __global__ void __launch_bounds__(kBlock) k_msb_pull_big(const uint2 *items, uint64_t nitems, const OffT *off,
                                                          const uint32_t *col, const u64 *F, const u64 *S, u64 *N,
-                                                         const u64 *live_in) {
+                                                         const u64 *live_in, uint32_t chunk) {
     constexpr int kU = 4;  // column loads in flight per lane
     u64 live[W];
 #pragma unroll
@@ -276,9 +275,9 @@ __global__ void __launch_bounds__(kBlock) k_msb_pull_big(const uint2 *items, uin
             none &= need[w] == 0ull;
         }
         if (none) continue;  // warp-uniform: every lane read the same words
-        OffT b = off[v] + (OffT)item.y * (OffT)kPullChunk;
+        OffT b = off[v] + (OffT)item.y * (OffT)chunk;
         OffT e = off[v + 1];
-        if (e - b > (OffT)kPullChunk) e = b + (OffT)kPullChunk;
+        if (e - b > (OffT)chunk) e = b + (OffT)chunk;
         u64 acc[W];
 #pragma unroll
         for (int w = 0; w < W; w++) acc[w] = 0;
@@ -523,16 +522,20 @@ void build_pull_items(ptg_graph *g) {
     unsigned long long *cnt = ctx->ws.bsum.as<unsigned long long>();
     int grid = grid_for(g->n, kBlock, ctx->sm_count * 8);
     PTG_CUDA_TRY(cudaMemsetAsync(cnt, 0, 8, st));
-    launch(ctx, "k_pull_items", k_pull_items<OffT>, grid, kBlock, 0, st, g->n, off, (uint2 *)nullptr, cnt);
+    const uint32_t small = ctx->tuning.ms_pull_small, chunk = ctx->tuning.ms_pull_chunk;
+    launch(ctx, "k_pull_items", k_pull_items<OffT>, grid, kBlock, 0, st, g->n, off, small, chunk, (uint2 *)nullptr,
+           cnt);
     unsigned long long total = 0;
     PTG_CUDA_TRY(cudaMemcpyAsync(&total, cnt, 8, cudaMemcpyDeviceToHost, st));
     PTG_CUDA_TRY(cudaStreamSynchronize(st));
     if (total) {
         g->d_pull_items.ensure(total * sizeof(uint2));
         PTG_CUDA_TRY(cudaMemsetAsync(cnt, 0, 8, st));
-        launch(ctx, "k_pull_items", k_pull_items<OffT>, grid, kBlock, 0, st, g->n, off,
+        launch(ctx, "k_pull_items", k_pull_items<OffT>, grid, kBlock, 0, st, g->n, off, small, chunk,
                g->d_pull_items.as<uint2>(), cnt);
     }
+    g->pull_small = small;
+    g->pull_chunk = chunk;
     g->n_pull_items = total;
     g->pull_items_built = true;
 }
@@ -606,11 +609,11 @@ void msbfs_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_ro
         PTG_CUDA_TRY(cudaMemsetAsync(Mn, 0, n * 8 * W, st));
         if (pull) {
             launch(ctx, "k_msb_pull_small", k_msb_pull_small<OffT, W>, vgrid, kBlock, 0, st, n, off, col,
-                   (const u64 *)Mc, (const u64 *)S, Mn, (const u64 *)d_live[cur]);
+                   (const u64 *)Mc, (const u64 *)S, Mn, (const u64 *)d_live[cur], g->pull_small);
             if (g->n_pull_items)
                 launch(ctx, "k_msb_pull_big", k_msb_pull_big<OffT, W>, sms * 8, kBlock, 0, st,
                        (const uint2 *)g->d_pull_items.p, g->n_pull_items, off, col, (const u64 *)Mc,
-                       (const u64 *)S, Mn, (const u64 *)d_live[cur]);
+                       (const u64 *)S, Mn, (const u64 *)d_live[cur], g->pull_chunk);
         } else {
             ms_scan<OffT>(ctx, ws, off, m, F, d_ctl);
             launch(ctx, "k_msb_push", k_msb_push<OffT, W>, sms * 8, kBlock, 0, st, (const uint32_t *)ws.q[0].p,

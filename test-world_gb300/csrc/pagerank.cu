@@ -133,12 +133,13 @@ __global__ void __launch_bounds__(kBlock) k_pr_init(const OffT *off, uint64_t n,
 }
 
 // ---------------------------------------------------------------------------
-// Degree-binned SpMV.  Rows are split once per graph by degree:
+// Degree-binned SpMV.  Rows are split once per graph by degree (mid and
+// chunk are tuning values, 64 and 4096 by default, recorded with the bins):
 //   deg <= kPrSmall          one thread per row (k_pr_small walks all rows)
-//   kPrSmall < deg <= kPrMid 8 lanes per row (list `mid`)
-//   kPrMid < deg <= kPrChunk one warp per row (list `big`)
-//   deg > kPrChunk           kPrChunk-edge chunks, one warp each, whose
-//                            partial sums are added in chunk order (k_pr_long)
+//   kPrSmall < deg <= mid    8 lanes per row (list `mid`)
+//   mid < deg <= chunk       one warp per row (list `big`)
+//   deg > chunk              chunk-edge pieces, one warp each, whose
+//                            partial sums are added in piece order (k_pr_long)
 // Every lane keeps its own two-float partial (independent dependency chains),
 // partials meet through shuffles in a fixed order, so a row's sum depends
 // only on the row.  No shared-memory staging and no CTA barriers; the lists
@@ -146,8 +147,6 @@ __global__ void __launch_bounds__(kBlock) k_pr_init(const OffT *off, uint64_t n,
 // neighbouring lanes fall in the same lines.
 // ---------------------------------------------------------------------------
 constexpr uint32_t kPrSmall = 4;
-constexpr uint32_t kPrMid = 64;
-constexpr uint32_t kPrChunk = 4096;
 
 struct PrBins {
     const uint32_t *mid;
@@ -159,6 +158,7 @@ struct PrBins {
     const uint2 *longs;  // (row, first item)
     uint64_t n_longs;
     float2 *partial;     // [n_items]
+    uint32_t chunk;      // edges per piece of a long row
 };
 
 __device__ __forceinline__ ff ff_shfl_xor(ff s, int o, int width) {
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_pr_big(PrArgs a, PrBins bins) {
     }
 }
 
-// Chunks of rows longer than kPrChunk: one warp per chunk, partial sums out.
+// Pieces of rows longer than bins.chunk: one warp per piece, partial sums out.
 template <class OffT>
 __global__ void __launch_bounds__(kBlock, 8) k_pr_chunks(PrArgs a, PrBins bins) {
     const OffT *off = reinterpret_cast<const OffT *>(a.off);
@@ -253,9 +253,9 @@ __global__ void __launch_bounds__(kBlock, 8) k_pr_chunks(PrArgs a, PrBins bins) 
     const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
     for (uint64_t it = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; it < bins.n_items; it += warps) {
         uint2 item = bins.items[it];
-        OffT b = off[item.x] + (OffT)item.y * (OffT)kPrChunk;
+        OffT b = off[item.x] + (OffT)item.y * (OffT)bins.chunk;
         OffT e = off[(uint64_t)item.x + 1];
-        if (e - b > (OffT)kPrChunk) e = b + (OffT)kPrChunk;
+        if (e - b > (OffT)bins.chunk) e = b + (OffT)bins.chunk;
         ff s{0.f, 0.f};
         OffT k = b + lane;
         for (; k + 96 < e; k += 128) {
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(kBlock) k_pr_long(PrArgs a, PrBins bins) {
          j += (uint64_t)gridDim.x * blockDim.x) {
         uint2 L = bins.longs[j];
         OffT deg = off[(uint64_t)L.x + 1] - off[L.x];
-        uint32_t pieces = (uint32_t)(((uint64_t)deg + kPrChunk - 1) / kPrChunk);
+        uint32_t pieces = (uint32_t)(((uint64_t)deg + bins.chunk - 1) / bins.chunk);
         ff s{0.f, 0.f};
         for (uint32_t i = 0; i < pieces; i++) {
             float2 p = bins.partial[(uint64_t)L.y + i];
@@ -435,9 +435,9 @@ __global__ void __launch_bounds__(kBlock) k_prk_chunks(MsArgs a, PrBins bins) {
     const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
     for (uint64_t it = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32; it < bins.n_items; it += warps) {
         uint2 item = bins.items[it];
-        OffT b = off[item.x] + (OffT)item.y * (OffT)kPrChunk;
+        OffT b = off[item.x] + (OffT)item.y * (OffT)bins.chunk;
         OffT e = off[(uint64_t)item.x + 1];
-        if (e - b > (OffT)kPrChunk) e = b + (OffT)kPrChunk;
+        if (e - b > (OffT)bins.chunk) e = b + (OffT)bins.chunk;
         ff acc[K];
 #pragma unroll
         for (int s = 0; s < K; s++) acc[s] = ff{0.f, 0.f};
@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(kBlock) k_prk_long(MsArgs a, PrBins bins) {
          j += (uint64_t)gridDim.x * blockDim.x) {
         uint2 L = bins.longs[j];
         OffT deg = off[(uint64_t)L.x + 1] - off[L.x];
-        uint32_t pieces = (uint32_t)(((uint64_t)deg + kPrChunk - 1) / kPrChunk);
+        uint32_t pieces = (uint32_t)(((uint64_t)deg + bins.chunk - 1) / bins.chunk);
         ff acc[K];
 #pragma unroll
         for (int s = 0; s < K; s++) acc[s] = ff{0.f, 0.f};
@@ -507,18 +507,19 @@ __global__ void __launch_bounds__(kBlock) k_prk_out(const float *rank, uint64_t 
 // CTA) so that each list keeps ascending row order.  counts[blk*4 + t]:
 // rows of `mid`, rows of `big`, rows of `longs`, chunk items.
 template <class OffT>
-__global__ void __launch_bounds__(kBlock) k_pr_bin_count(const OffT *off, uint64_t n, unsigned long long *counts) {
+__global__ void __launch_bounds__(kBlock) k_pr_bin_count(const OffT *off, uint64_t n, uint32_t mid, uint32_t chunk,
+                                                         unsigned long long *counts) {
     uint64_t per = (n + gridDim.x - 1) / gridDim.x;
     uint64_t v0 = blockIdx.x * per, v1 = min(n, v0 + per);
     unsigned long long cm = 0, cb = 0, cl = 0, ci = 0;
     for (uint64_t v = v0 + threadIdx.x; v < v1; v += blockDim.x) {
         uint64_t deg = (uint64_t)(off[v + 1] - off[v]);
         if (deg <= kPrSmall) continue;
-        if (deg <= kPrMid) cm++;
-        else if (deg <= kPrChunk) cb++;
+        if (deg <= mid) cm++;
+        else if (deg <= chunk) cb++;
         else {
             cl++;
-            ci += (deg + kPrChunk - 1) / kPrChunk;
+            ci += (deg + chunk - 1) / chunk;
         }
     }
     cm = block_reduce_sum(cm);
@@ -534,8 +535,9 @@ __global__ void __launch_bounds__(kBlock) k_pr_bin_count(const OffT *off, uint64
 }
 
 template <class OffT>
-__global__ void __launch_bounds__(kBlock) k_pr_bin_fill(const OffT *off, uint64_t n, const unsigned long long *base,
-                                                        uint32_t *mid, uint32_t *big, uint2 *longs, uint2 *items) {
+__global__ void __launch_bounds__(kBlock) k_pr_bin_fill(const OffT *off, uint64_t n, uint32_t tmid, uint32_t chunk,
+                                                        const unsigned long long *base, uint32_t *mid, uint32_t *big,
+                                                        uint2 *longs, uint2 *items) {
     uint64_t per = (n + gridDim.x - 1) / gridDim.x;
     uint64_t v0 = blockIdx.x * per, v1 = min(n, v0 + per);
     unsigned long long bm = base[blockIdx.x * 4 + 0], bb = base[blockIdx.x * 4 + 1];
@@ -543,8 +545,8 @@ __global__ void __launch_bounds__(kBlock) k_pr_bin_fill(const OffT *off, uint64_
     for (uint64_t c0 = v0; c0 < v1; c0 += blockDim.x) {
         uint64_t v = c0 + threadIdx.x;
         uint64_t deg = v < v1 ? (uint64_t)(off[v + 1] - off[v]) : 0;
-        unsigned long long fm = deg > kPrSmall && deg <= kPrMid, fb = deg > kPrMid && deg <= kPrChunk;
-        unsigned long long fl = deg > kPrChunk, fi = fl ? (deg + kPrChunk - 1) / kPrChunk : 0;
+        unsigned long long fm = deg > kPrSmall && deg <= tmid, fb = deg > tmid && deg <= chunk;
+        unsigned long long fl = deg > chunk, fi = fl ? (deg + chunk - 1) / chunk : 0;
         unsigned long long tm, tb, tl, ti;
         unsigned long long pm = block_exclusive_scan(fm, tm);
         unsigned long long pb = block_exclusive_scan(fb, tb);
@@ -571,7 +573,8 @@ void build_pr_bins(ptg_graph *g) {
     const int nb = (int)std::min<uint64_t>(1024, std::max<uint64_t>(1, (g->n + kBlock - 1) / kBlock));
     DevBuf counts;
     counts.ensure((uint64_t)nb * 4 * 8);
-    launch(ctx, "k_pr_bin_count", k_pr_bin_count<OffT>, nb, kBlock, 0, st, off, g->n,
+    const uint32_t mid = ctx->tuning.pr_mid, chunk = ctx->tuning.pr_chunk;
+    launch(ctx, "k_pr_bin_count", k_pr_bin_count<OffT>, nb, kBlock, 0, st, off, g->n, mid, chunk,
            counts.as<unsigned long long>());
     std::vector<unsigned long long> h((size_t)nb * 4);
     PTG_CUDA_TRY(cudaMemcpyAsync(h.data(), counts.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
@@ -588,7 +591,7 @@ void build_pr_bins(ptg_graph *g) {
     g->d_pr_big.ensure(std::max<unsigned long long>(tot[1], 1) * 4);
     g->d_pr_longs.ensure(std::max<unsigned long long>(tot[2], 1) * 8);
     g->d_pr_items.ensure(std::max<unsigned long long>(tot[3], 1) * 8);
-    launch(ctx, "k_pr_bin_fill", k_pr_bin_fill<OffT>, nb, kBlock, 0, st, off, g->n,
+    launch(ctx, "k_pr_bin_fill", k_pr_bin_fill<OffT>, nb, kBlock, 0, st, off, g->n, mid, chunk,
            (const unsigned long long *)counts.p, g->d_pr_mid.as<uint32_t>(), g->d_pr_big.as<uint32_t>(),
            g->d_pr_longs.as<uint2>(), g->d_pr_items.as<uint2>());
     PTG_CUDA_TRY(cudaStreamSynchronize(st));
@@ -596,6 +599,8 @@ void build_pr_bins(ptg_graph *g) {
     g->n_pr_big = tot[1];
     g->n_pr_longs = tot[2];
     g->n_pr_items = tot[3];
+    g->pr_mid = mid;
+    g->pr_chunk = chunk;
     g->pr_bins_built = true;
 }
 
@@ -628,6 +633,8 @@ void pagerank_impl(ptg_graph *g, bool personalized, uint32_t src, double damping
     bins.longs = g->d_pr_longs.as<uint2>();
     bins.n_longs = g->n_pr_longs;
     bins.partial = ws.aux.as<float2>();
+    bins.chunk = g->pr_chunk;
+    const int pcap = sms * (int)ctx->tuning.pr_ctas_per_sm;
     for (uint32_t it = 0; it < iters; it++) {
         int cin = it & 1, cout = cin ^ 1;
         PTG_CUDA_TRY(cudaMemsetAsync(&dang[cout], 0, 8, st));
@@ -644,15 +651,15 @@ void pagerank_impl(ptg_graph *g, bool personalized, uint32_t src, double damping
         a.d = damping;
         a.personalized = personalized ? 1 : 0;
         a.src = src;
-        launch(ctx, "k_pr_small", k_pr_small<OffT>, fill_grid, kBlock, 0, st, a);
+        launch(ctx, "k_pr_small", k_pr_small<OffT>, grid_for(n, kBlock, pcap), kBlock, 0, st, a);
         if (bins.n_mid)
-            launch(ctx, "k_pr_mid", k_pr_mid<OffT>, grid_for(bins.n_mid * 8, kBlock, sms * 8), kBlock, 0, st, a,
+            launch(ctx, "k_pr_mid", k_pr_mid<OffT>, grid_for(bins.n_mid * 8, kBlock, pcap), kBlock, 0, st, a,
                    bins);
         if (bins.n_big)
-            launch(ctx, "k_pr_big", k_pr_big<OffT>, grid_for(bins.n_big * 32, kBlock, sms * 8), kBlock, 0, st, a,
+            launch(ctx, "k_pr_big", k_pr_big<OffT>, grid_for(bins.n_big * 32, kBlock, pcap), kBlock, 0, st, a,
                    bins);
         if (bins.n_items) {
-            launch(ctx, "k_pr_chunks", k_pr_chunks<OffT>, grid_for(bins.n_items * 32, kBlock, sms * 8), kBlock,
+            launch(ctx, "k_pr_chunks", k_pr_chunks<OffT>, grid_for(bins.n_items * 32, kBlock, pcap), kBlock,
                    0, st, a, bins);
             launch(ctx, "k_pr_long", k_pr_long<OffT>, grid_for(bins.n_longs, kBlock, sms * 2), kBlock, 0, st, a,
                    bins);
@@ -694,7 +701,8 @@ void ppr_multi_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, float *d_r
     bins.longs = g->d_pr_longs.as<uint2>();
     bins.n_longs = g->n_pr_longs;
     bins.partial = ws.aux.as<float2>();
-    int fill_grid = grid_for(n, kBlock, sms * 8);
+    bins.chunk = g->pr_chunk;
+    const int pcap = sms * (int)ctx->tuning.pr_ctas_per_sm;
     for (uint32_t it = 0; it < iters; it++) {
         int cin = it & 1, cout = cin ^ 1;
         PTG_CUDA_TRY(cudaMemsetAsync(dang + cout * K, 0, K * 8, st));
@@ -709,15 +717,15 @@ void ppr_multi_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, float *d_r
         a.src = d_src;
         a.d = damping;
         a.last = it + 1 == iters;
-        launch(ctx, "k_prk_small", k_prk_small<OffT, K>, fill_grid, kBlock, 0, st, a);
+        launch(ctx, "k_prk_small", k_prk_small<OffT, K>, grid_for(n, kBlock, pcap), kBlock, 0, st, a);
         if (bins.n_mid)
-            launch(ctx, "k_prk_mid", k_prk_mid<OffT, K>, grid_for(bins.n_mid * 8, kBlock, sms * 8), kBlock, 0, st, a,
+            launch(ctx, "k_prk_mid", k_prk_mid<OffT, K>, grid_for(bins.n_mid * 8, kBlock, pcap), kBlock, 0, st, a,
                    bins);
         if (bins.n_big)
-            launch(ctx, "k_prk_big", k_prk_big<OffT, K>, grid_for(bins.n_big * 32, kBlock, sms * 8), kBlock, 0, st, a,
+            launch(ctx, "k_prk_big", k_prk_big<OffT, K>, grid_for(bins.n_big * 32, kBlock, pcap), kBlock, 0, st, a,
                    bins);
         if (bins.n_items) {
-            launch(ctx, "k_prk_chunks", k_prk_chunks<OffT, K>, grid_for(bins.n_items * 32, kBlock, sms * 8), kBlock,
+            launch(ctx, "k_prk_chunks", k_prk_chunks<OffT, K>, grid_for(bins.n_items * 32, kBlock, pcap), kBlock,
                    0, st, a, bins);
             launch(ctx, "k_prk_long", k_prk_long<OffT, K>, grid_for(bins.n_longs, kBlock, sms * 2), kBlock, 0, st, a,
                    bins);

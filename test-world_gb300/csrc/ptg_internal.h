@@ -225,6 +225,7 @@ struct ptg_ctx {
     std::string last_error;
     ptg::Prof prof;
     ptg::Workspace ws;
+    ptg_tuning tuning;                   // ptg_tuning_defaults at creation
 };
 
 namespace ptg {
@@ -252,9 +253,11 @@ struct ptg_graph {
     ptg::DevBuf d_pull_items;  // (vertex, chunk) work items of high-degree vertices (multi-source pull)
     uint64_t n_pull_items = 0;
     bool pull_items_built = false;
+    uint32_t pull_small = 0, pull_chunk = 0;  // the thresholds the pull items were built with
     ptg::DevBuf d_pr_mid, d_pr_big, d_pr_items, d_pr_longs;  // PageRank rows binned by degree
     uint64_t n_pr_mid = 0, n_pr_big = 0, n_pr_items = 0, n_pr_longs = 0;
     bool pr_bins_built = false;
+    uint32_t pr_mid = 0, pr_chunk = 0;  // the thresholds the bins were built with
     // out-of-core
     bool out_of_core = false;
     uint64_t resident_edges = 0;

@@ -127,6 +127,10 @@ ptg_graph *make_view(ptg_graph *g, ptg_ctx *lane) {
     alias(v->d_pull_items, g->d_pull_items);
     v->n_pull_items = g->n_pull_items;
     v->pull_items_built = g->pull_items_built;
+    v->pull_small = g->pull_small;
+    v->pull_chunk = g->pull_chunk;
+    v->pr_mid = g->pr_mid;
+    v->pr_chunk = g->pr_chunk;
     v->n_pr_mid = g->n_pr_mid;
     v->n_pr_big = g->n_pr_big;
     v->n_pr_items = g->n_pr_items;
@@ -511,6 +515,7 @@ ptg_status ptg_server_create(ptg_ctx *ctx, const ptg_server_config *cfg, ptg_ser
             delete s;
             return st;
         }
+        L->ctx->tuning = ctx->tuning;  // lanes run with the creating context's tuning
         s->lanes.push_back(std::move(L));
     }
     for (size_t i = 0; i < s->lanes.size(); i++) s->lanes[i]->th = std::thread(lane_loop, s, i);

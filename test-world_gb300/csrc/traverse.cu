@@ -615,7 +615,9 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
     // relaxes in label-correcting rounds unless a bucket width is asked for
     // (RMAT-26 all streamed: 9 rounds and 55 GB over the link instead of 18
     // rounds and 107 GB).
-    bool use_far = kind == TRAV_SSSP && !(flags & PTG_REFERENCE_SCHEDULE) && (!g->out_of_core || delta != 0);
+    const ptg_tuning &tu = ctx->tuning;
+    bool use_far = kind == TRAV_SSSP && !(flags & PTG_REFERENCE_SCHEDULE) &&
+                   (delta != 0 || (!g->out_of_core && tu.sssp_delta_scale > 0.f));
     if (use_far) ws.farbm.ensure(words * 4);
     TravCtl *d_ctl = ws.ctl.as<TravCtl>();
     TravCtl *h_ctl = ws.h_ctl.as<TravCtl>();
@@ -644,9 +646,11 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         init.level_val = base;
         if (use_far) {
             if (delta == 0) {
-                // default bucket width: half the mean edge weight (measured once per graph)
+                // default bucket width: a tuned fraction (half) of the mean edge
+                // weight, measured once per graph
                 measure_mean_weight(g);
-                delta = (uint32_t)std::max(1.0, g->mean_weight > 0 ? g->mean_weight / 2 : 32.0);
+                double scale = tu.sssp_delta_scale;
+                delta = (uint32_t)std::min(1e9, std::max(1.0, g->mean_weight > 0 ? g->mean_weight * scale : 64.0 * scale));
             }
             init.threshold = base + delta;
             PTG_CUDA_TRY(cudaMemsetAsync(ws.farbm.p, 0, words * 4, st));
@@ -677,7 +681,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
     uint32_t threshold = init.threshold, level_val = base;
     bool bottom_up = false;
     if (max_iters == 0) max_iters = (uint32_t)std::min<uint64_t>(0xFFFFFFF0ull, 4 * n + 16);
-    const double alpha = 15.0, beta = 18.0;
+    const double alpha = tu.bfs_alpha, beta = tu.bfs_beta;
 
     bool link_open = false;  // a level's copies were recorded between link_ev[0] and link_ev[1]
     // out-of-core staging
@@ -757,8 +761,9 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
             if (!small)
                 launch(ctx, "k_scan_write", k_scan_write<OffT>, scan_blocks, kBlock, 0, st, q_cur, d_ctl, off,
                        clip, bsum, sc, rs);
-            int eg = sms * 8;
-            if (allow_bu) eg = grid_for(E, kTile, sms * 8);
+            const int ecap = sms * (int)tu.expand_ctas_per_sm;
+            int eg = ecap;
+            if (allow_bu) eg = grid_for(E, kTile, ecap);
             uint32_t *tr = ws.tiles.as<uint32_t>();
             launch(ctx, "k_tile_rows", k_tile_rows<OffT>, allow_bu ? grid_for(E / kTile + 1, kBlock, sms * 4) : sms * 4,
                    kBlock, 0, st, sc, d_ctl, tr);

@@ -117,8 +117,53 @@ class ServerStats(ctypes.Structure):
                 ("single_ms", ctypes.c_double * 3)]
 
 
+PTG_TUNING_VERSION = 1
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("version", ctypes.c_uint32), ("bfs_alpha", ctypes.c_float), ("bfs_beta", ctypes.c_float),
+                ("sssp_delta_scale", ctypes.c_float), ("expand_ctas_per_sm", ctypes.c_uint32),
+                ("pr_ctas_per_sm", ctypes.c_uint32), ("pr_mid", ctypes.c_uint32), ("pr_chunk", ctypes.c_uint32),
+                ("ms_pull_small", ctypes.c_uint32), ("ms_pull_chunk", ctypes.c_uint32),
+                ("reserved0", ctypes.c_uint32 * 2), ("partition_bytes", ctypes.c_uint64),
+                ("reserved", ctypes.c_uint32 * 8)]
+
+    KNOBS = ("bfs_alpha", "bfs_beta", "sssp_delta_scale", "expand_ctas_per_sm", "pr_ctas_per_sm", "pr_mid",
+             "pr_chunk", "ms_pull_small", "ms_pull_chunk", "partition_bytes")
+
+    def as_dict(self):
+        return {k: (round(float(getattr(self, k)), 6) if isinstance(getattr(self, k), float) else int(getattr(self, k)))
+                for k in self.KNOBS}
+
+
+def tuning_defaults():
+    """The built-in tuning values as a dict (no GPU needed)."""
+    t = Tuning()
+    lib().ptg_tuning_defaults(ctypes.byref(t))
+    return t.as_dict()
+
+
+def _tuning_struct(values):
+    t = Tuning()
+    lib().ptg_tuning_defaults(ctypes.byref(t))
+    for k, v in values.items():
+        if k not in Tuning.KNOBS:
+            raise KeyError("unknown tuning knob %r" % k)
+        setattr(t, k, v)
+    return t
+
+
+def tuning_valid(values):
+    """True if the library accepts these knob values (no GPU needed)."""
+    return lib().ptg_tuning_validate(ctypes.byref(_tuning_struct(values))) == PTG_OK
+
+
 # Every function the header declares, with its ctypes signature.
 _SIGS = {
+    "ptg_tuning_defaults": (None, [ctypes.POINTER(Tuning)]),
+    "ptg_tuning_validate": (ctypes.c_int, [ctypes.POINTER(Tuning)]),
+    "ptg_ctx_set_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(Tuning)]),
+    "ptg_ctx_get_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(Tuning)]),
     "ptg_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "ptg_partition_config_default": (None, [ctypes.POINTER(PartitionConfig)]),
     "ptg_plan_partitions": (ctypes.c_int, [ctypes.c_uint64, ctypes.c_uint64, _u64p, ctypes.c_uint64,
@@ -234,6 +279,7 @@ class Ctx:
     """A context on one CUDA device (owns streams and reusable workspace)."""
 
     def __init__(self, device=0):
+        self.device = device
         self.h = _vp()
         self._deps = weakref.WeakSet()  # graphs and servers, closed before the context
         _check(lib().ptg_ctx_create(device, ctypes.byref(self.h)))
@@ -259,6 +305,26 @@ class Ctx:
         _check(lib().ptg_ctx_device_info(self.h, ctypes.byref(sms), ctypes.byref(hbm),
                                          ctypes.byref(free)), self.h)
         return {"sm_count": sms.value, "hbm_bytes": hbm.value, "free_bytes": free.value}
+
+    def tuning(self):
+        """The context's tuning knobs as a dict."""
+        t = Tuning()
+        _check(lib().ptg_ctx_get_tuning(self.h, ctypes.byref(t)), self.h)
+        return t.as_dict()
+
+    def set_tuning(self, values=None, **kw):
+        """Apply tuning knobs (unnamed ones take the built-in defaults)."""
+        v = dict(values or {})
+        v.update(kw)
+        _check(lib().ptg_ctx_set_tuning(self.h, ctypes.byref(_tuning_struct(v))), self.h)
+
+    def load_tuning(self, path):
+        """Apply the "tuning" object of an autotuner JSON file (ptgraph.tune)."""
+        import json
+        with open(path) as f:
+            doc = json.load(f)
+        self.set_tuning(doc.get("tuning", doc))
+        return self.tuning()
 
     def profile(self, enable=True):
         """Enable/disable per-kernel CUDA-event timing (clears the totals)."""
@@ -417,9 +483,9 @@ class Graph:
             stats.update(st.as_dict())
         return out
 
-    def msbfs(self, sources, flags=0, stats=None):
+    def msbfs(self, sources, flags=0, stats=None, out=None):
         s = np.ascontiguousarray(sources, dtype=np.uint32)
-        out = np.empty((s.size, self.n), dtype=np.uint32)
+        out = np.empty((s.size, self.n), dtype=np.uint32) if out is None else out
         o, st = self._opts(flags, 0, stats)
         _check(lib().ptg_msbfs(self.h, s.ctypes.data_as(_u32p), s.size, _ptr(out), ctypes.byref(o)),
                self.ctx.h)
@@ -427,9 +493,9 @@ class Graph:
             stats.update(st.as_dict())
         return out
 
-    def mssssp(self, sources, flags=0, stats=None):
+    def mssssp(self, sources, flags=0, stats=None, out=None):
         s = np.ascontiguousarray(sources, dtype=np.uint32)
-        out = np.empty((s.size, self.n), dtype=np.uint32)
+        out = np.empty((s.size, self.n), dtype=np.uint32) if out is None else out
         o, st = self._opts(flags, 0, stats)
         _check(lib().ptg_mssssp(self.h, s.ctypes.data_as(_u32p), s.size, _ptr(out), ctypes.byref(o)),
                self.ctx.h)

@@ -1,0 +1,147 @@
+"""Tuning knobs (ptg_tuning) and the autotuner (ptgraph.tune).
+
+CPU: the built-in values, range validation and the JSON round trip.
+GPU: every algorithm keeps its results under non-default knobs (integer
+results bit-exact vs the oracle, PageRank within 1e-6 of the FP64 oracle,
+batched PPR rows identical to single PPR), the tuned partition size is the one
+an out-of-core graph gets, and a small autotuner run writes a loadable file."""
+import json
+import math
+
+import numpy as np
+import pytest
+
+PR_RTOL = 1e-6  # max per-vertex relative error vs the FP64 oracle
+
+# every knob away from its default (and inside its range)
+OFF_DEFAULT = {"bfs_alpha": 6.0, "bfs_beta": 36.0, "sssp_delta_scale": 2.0, "expand_ctas_per_sm": 3,
+               "pr_ctas_per_sm": 5, "pr_mid": 16, "pr_chunk": 1024, "ms_pull_small": 8, "ms_pull_chunk": 256,
+               "partition_bytes": 1 << 20}
+
+
+def test_builtin_values(ptg):
+    d = ptg.tuning_defaults()
+    assert d == {"bfs_alpha": 15.0, "bfs_beta": 18.0, "sssp_delta_scale": 0.5, "expand_ctas_per_sm": 8,
+                 "pr_ctas_per_sm": 8, "pr_mid": 64, "pr_chunk": 4096, "ms_pull_small": 32,
+                 "ms_pull_chunk": 1024, "partition_bytes": 256 << 20}
+    assert ptg.tuning_valid(d)
+    assert ptg.tuning_valid(OFF_DEFAULT)
+
+
+@pytest.mark.parametrize("bad", [
+    {"pr_mid": 4}, {"pr_mid": 8192}, {"pr_chunk": 100}, {"pr_chunk": 1 << 17},
+    {"ms_pull_chunk": 100}, {"ms_pull_chunk": 16}, {"ms_pull_small": 0}, {"ms_pull_small": 5000},
+    {"expand_ctas_per_sm": 0}, {"expand_ctas_per_sm": 33}, {"pr_ctas_per_sm": 0},
+    {"bfs_alpha": 0.0}, {"bfs_alpha": math.nan}, {"bfs_beta": math.inf}, {"sssp_delta_scale": -1.0},
+    {"partition_bytes": 4096}, {"partition_bytes": 1 << 40},
+])
+def test_out_of_range_rejected(ptg, bad):
+    assert not ptg.tuning_valid(bad)
+
+
+def test_version_checked(ptg):
+    import ctypes
+    t = ptg._tuning_struct({})
+    assert ptg.lib().ptg_tuning_validate(ctypes.byref(t)) == ptg.PTG_OK
+    t.version = 2
+    assert ptg.lib().ptg_tuning_validate(ctypes.byref(t)) == ptg.PTG_ERR_INVALID
+    assert ptg.lib().ptg_tuning_validate(None) == ptg.PTG_ERR_INVALID
+
+
+def test_unknown_knob_rejected(ptg):
+    with pytest.raises(KeyError):
+        ptg.tuning_valid({"warp_size": 64})
+
+
+def test_candidates_valid_and_json_round_trip(ptg, tmp_path):
+    from ptgraph import tune
+    d = ptg.tuning_defaults()
+    assert set(tune.CANDIDATES) == set(d) == set(tune.WORKLOAD)
+    for knob, values in tune.CANDIDATES.items():
+        assert d[knob] in values  # the built-in value is always among the candidates
+        for v in values:
+            t = dict(d)
+            t[knob] = v
+            assert ptg.tuning_valid(t), (knob, v)
+    path = tmp_path / "t.json"
+    path.write_text(json.dumps({"version": 1, "tuning": OFF_DEFAULT}))
+    doc = json.loads(path.read_text())
+    assert ptg._tuning_struct(doc["tuning"]).as_dict() == OFF_DEFAULT
+
+
+# ----------------------------------------------------------------------------
+# GPU
+# ----------------------------------------------------------------------------
+
+@pytest.fixture(scope="module")
+def tctx(ptg):
+    c = ptg.Ctx(0)  # its own context: the shared one keeps the built-in tuning
+    yield c
+    c.close()
+
+
+@pytest.mark.gpu
+def test_results_unchanged_under_other_knobs(ptg, oracle, tctx):
+    import torch
+    tctx.set_tuning(OFF_DEFAULT)
+    assert tctx.tuning() == OFF_DEFAULT
+    off, col, w = ptg.gen_rmat(14, 16, seed=11, symmetric=True, wmin=1, wmax=63)
+    G = tctx.graph(off, col, w, symmetric=True)
+    deg = np.diff(off.astype(np.int64))
+    srcs = np.random.default_rng(3).choice(np.nonzero(deg)[0], 6, replace=False).astype(np.uint32)
+    for s in srcs[:3]:
+        s = int(s)
+        assert (G.bfs(s) == oracle.bfs(off, col, s, method="queue")).all()
+        assert (G.sssp(s) == oracle.sssp(off, col, w, s)).all()
+    assert (G.cc() == oracle.cc(off, col, method="unionfind")).all()
+    r = G.pagerank().astype(np.float64)
+    ref = oracle.pagerank(off, col)
+    assert (np.abs(r - ref) / ref).max() < PR_RTOL
+    single = [G.ppr(int(s)) for s in srcs]
+    batch = G.ppr_batch(srcs)
+    for i, s in enumerate(srcs):
+        assert np.array_equal(batch[i], single[i])  # same bins, same order: bit-identical
+        pref = oracle.ppr(off, col, int(s))
+        nz = pref > 1e-30
+        assert (np.abs(single[i][nz] - pref[nz]) / pref[nz]).max() < PR_RTOL
+    ms = G.msbfs(srcs)
+    for i, s in enumerate(srcs):
+        assert (ms[i] == oracle.bfs(off, col, int(s), method="queue")).all()
+    # device outputs as the autotuner times them
+    out = torch.empty(G.n, dtype=torch.int32, device="cuda")
+    G.bfs(int(srcs[0]), flags=ptg.PTG_OUT_DEVICE, out=out)
+    assert (out.cpu().numpy().view(np.uint32) == oracle.bfs(off, col, int(srcs[0]), method="queue")).all()
+    G.close()
+    # partitions of a graph created without a partition size take the tuned one
+    offd, cold, wd = ptg.gen_rmat(14, 16, seed=12, symmetric=False, wmin=1, wmax=63)
+    cfg = ptg.partition_config(force_out_of_core=1, device_budget_bytes=1 << 20)
+    assert cfg.partition_bytes == 0
+    Gd = tctx.graph(offd, cold, wd, config=cfg)
+    info = Gd.info()
+    assert info["out_of_core"] == 1 and info["partition_edges"] == (1 << 20) // 8
+    assert (Gd.sssp(0) == oracle.sssp(offd, cold, wd, 0)).all()
+    Gd.close()
+    tctx.set_tuning()
+    assert tctx.tuning() == ptg.tuning_defaults()
+
+
+@pytest.mark.gpu
+def test_autotuner_small_run(ptg, tctx, tmp_path):
+    from ptgraph import tune
+    knobs = ["pr_mid", "bfs_alpha", "expand_ctas_per_sm", "sssp_delta_scale", "ms_pull_small",
+             "partition_bytes"]
+    doc = tune.tune(tctx, scale=13, repeats=1, knobs=knobs, n_bfs=4, n_sssp=2, n_ms=16, ooc_scale=15,
+                    log=lambda *a: None)
+    assert set(doc["sweeps"]) == set(knobs)
+    for k in knobs:
+        rows = doc["sweeps"][k]["candidates"]
+        assert len(rows) == len(tune.CANDIDATES[k])
+        assert all(r["same_result"] for r in rows if r["ms"] is not None)
+        assert doc["tuning"][k] in tune.CANDIDATES[k]
+    assert ptg.tuning_valid(doc["tuning"])
+    assert tctx.tuning() == doc["tuning"]  # left applied
+    path = tmp_path / "tuning.json"
+    path.write_text(json.dumps(doc))
+    tctx.set_tuning()
+    assert tctx.load_tuning(str(path)) == doc["tuning"]
+    tctx.set_tuning()
