@@ -232,7 +232,10 @@ typedef struct ptg_tuning {
                                     a thread, longer ones warps (default 32; 1..4096)    */
     uint32_t ms_pull_chunk;      /* edges per warp item of a long row (default 1024;
                                     32..65536, a multiple of 32)                         */
-    uint32_t reserved0[2];       /* zero; keeps partition_bytes at byte offset 48       */
+    uint32_t vertex_order;       /* 1: resident symmetric graphs are stored with their
+                                    vertices grouped by degree (ids are mapped in and
+                                    out; results are unchanged); 0: as given (default 1)*/
+    uint32_t reserved0;          /* zero; keeps partition_bytes at byte offset 48       */
     uint64_t partition_bytes;    /* edge bytes per partition of an out-of-core graph
                                     created without a partition size (default 256 MiB;
                                     1 MiB..16 GiB)                                       */

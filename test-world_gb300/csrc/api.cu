@@ -248,6 +248,7 @@ void ptg_tuning_defaults(ptg_tuning *t) {
     t->pr_chunk = 4096;
     t->ms_pull_small = 32;
     t->ms_pull_chunk = 1024;
+    t->vertex_order = 1;
     t->partition_bytes = 256ull << 20;
 }
 
@@ -262,6 +263,7 @@ ptg_status ptg_tuning_validate(const ptg_tuning *t) {
     if (t->pr_mid < 8 || t->pr_mid > t->pr_chunk) return PTG_ERR_INVALID;
     if (t->ms_pull_small < 1 || t->ms_pull_small > 4096) return PTG_ERR_INVALID;
     if (t->ms_pull_chunk < 32 || t->ms_pull_chunk > 65536 || t->ms_pull_chunk % 32) return PTG_ERR_INVALID;
+    if (t->vertex_order > 1) return PTG_ERR_INVALID;
     if (t->partition_bytes < (1ull << 20) || t->partition_bytes > (16ull << 30)) return PTG_ERR_INVALID;
     return PTG_OK;
 }
@@ -493,6 +495,7 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
         PTG_CUDA_TRY(cudaStreamSynchronize(st));
         PTG_REQUIRE(!(hbad & 1), PTG_ERR_INVALID, "offsets are not non-decreasing within [0, m]");
         PTG_REQUIRE(!(hbad & 2), PTG_ERR_INVALID, "an edge target is >= n");
+        relabel_graph(g);  // degree-grouped vertex order, when the tuning asks for it
 
         if (g->out_of_core) {
             // host side of the streamed partitions: pinned SoA arrays

@@ -276,6 +276,13 @@ void run_cc_hook(ptg_graph *g, uint32_t *d_label, RunResult &rr) {
     if (!g->out_of_core && g->m > 0) {
         // resident symmetric graph: Afforest
         Workspace &ws = g->ctx->ws;
+        uint32_t *out = d_label;
+        if (g->relabeled) {
+            // labels in the stored vertex order first, then the minimum caller id per component
+            ws.relab[0].ensure(g->n * 4);
+            ws.relab[1].ensure(g->n * 4);
+            d_label = ws.relab[0].as<uint32_t>();
+        }
         ws.bsum.ensure(1024 * 8);
         uint64_t *d_vb = ws.bsum.as<uint64_t>();
         uint32_t *d_giant = reinterpret_cast<uint32_t *>(d_vb + 2);
@@ -288,6 +295,7 @@ void run_cc_hook(ptg_graph *g, uint32_t *d_label, RunResult &rr) {
         else
             afforest<uint32_t>(g->ctx, g->d_off.as<uint32_t>(), g->d_col.as<uint32_t>(), g->n, g->m, d_vb, 1,
                                d_label, d_giant, d_counter);
+        if (g->relabeled) cc_labels_out(g, d_label, ws.relab[1].as<uint32_t>(), out);
         rr.edges_relaxed = g->m;
         rr.iterations = 1;
         return;

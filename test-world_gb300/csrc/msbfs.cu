@@ -444,14 +444,16 @@ __global__ void __launch_bounds__(kBlock) k_mss_relax(const uint32_t *q, const O
     }
 }
 
-// dist[v*64 + s] -> out[s*n + v] for s < k (32 vertices x 64 sources per tile).
+// dist[x*64 + s] -> out[s*n + v] for s < k (32 vertices x 64 sources per
+// tile), x = newid[v] on a regrouped graph (else v).
 __global__ void __launch_bounds__(kBlock) k_mss_transpose(const uint32_t *dist, uint64_t n, uint32_t k,
-                                                          uint32_t *out) {
+                                                          const uint32_t *newid, uint32_t *out) {
     __shared__ uint32_t t[32][65];
     for (uint64_t v0 = (uint64_t)blockIdx.x * 32; v0 < n; v0 += (uint64_t)gridDim.x * 32) {
         for (int i = threadIdx.x; i < 32 * 64; i += kBlock) {
             int vv = i / 64, s = i % 64;
-            t[vv][s] = v0 + vv < n ? dist[(v0 + vv) * 64 + s] : 0u;
+            uint64_t x = v0 + vv < n ? (newid ? (uint64_t)newid[v0 + vv] : v0 + vv) : 0;
+            t[vv][s] = v0 + vv < n ? dist[x * 64 + s] : 0u;
         }
         __syncthreads();
         for (int i = threadIdx.x; i < 32 * 64; i += kBlock) {
@@ -584,6 +586,7 @@ void msbfs_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_ro
         all[w] = bits == 64 ? ~0ull : ((1ull << bits) - 1ull);
     }
     PTG_CUDA_TRY(cudaMemcpyAsync(d_srcs, h_srcs, k * 4, cudaMemcpyHostToDevice, st));
+    map_sources_dev(g, d_srcs, k);
     PTG_CUDA_TRY(cudaMemcpyAsync(d_all, all, sizeof(all), cudaMemcpyHostToDevice, st));
     launch(ctx, "k_msb_seed", k_msb_seed<W>, 1, 256, 0, st, (const uint32_t *)d_srcs, k, M0, S, d_rows, n, base);
     TravCtl init{};
@@ -653,6 +656,7 @@ void mssssp_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_r
     PTG_CUDA_TRY(cudaMemsetAsync(M0, 0, n * 8, st));
     PTG_CUDA_TRY(cudaMemsetAsync(M1, 0, n * 8, st));
     PTG_CUDA_TRY(cudaMemcpyAsync(d_srcs, h_srcs, k * 4, cudaMemcpyHostToDevice, st));
+    map_sources_dev(g, d_srcs, k);
     launch(ctx, "k_mss_seed", k_mss_seed, 1, 64, 0, st, (const uint32_t *)d_srcs, k, M0, dist, base);
     TravCtl init{};
     PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &init, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
@@ -680,7 +684,7 @@ void mssssp_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_r
         cur ^= 1;
     }
     launch(ctx, "k_mss_transpose", k_mss_transpose, grid_for((n + 31) / 32, 1, sms * 8), kBlock, 0, st,
-           (const uint32_t *)dist, n, k, d_rows);
+           (const uint32_t *)dist, n, k, (const uint32_t *)(g->relabeled ? g->d_newid.p : nullptr), d_rows);
     PTG_CUDA_TRY(cudaGetLastError());
     (void)Eact;
 }
@@ -708,15 +712,25 @@ bool ms_group(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, uint32_t *d_rows
     if (weighted) {
         if (o64) mssssp_impl<unsigned long long>(g, h_srcs, k, d_rows, flags, rr);
         else mssssp_impl<uint32_t>(g, h_srcs, k, d_rows, flags, rr);
-    } else if (k <= 64) {
-        if (o64) msbfs_impl<unsigned long long, 1>(g, h_srcs, k, d_rows, flags, rr);
-        else msbfs_impl<uint32_t, 1>(g, h_srcs, k, d_rows, flags, rr);
-    } else if (k <= 128) {
-        if (o64) msbfs_impl<unsigned long long, 2>(g, h_srcs, k, d_rows, flags, rr);
-        else msbfs_impl<uint32_t, 2>(g, h_srcs, k, d_rows, flags, rr);
     } else {
-        if (o64) msbfs_impl<unsigned long long, 4>(g, h_srcs, k, d_rows, flags, rr);
-        else msbfs_impl<uint32_t, 4>(g, h_srcs, k, d_rows, flags, rr);
+        // levels are written as vertices are reached: into rows in the stored
+        // vertex order first on a regrouped graph, mapped to caller ids after
+        uint32_t *rows = d_rows;
+        if (g->relabeled) {
+            g->ctx->ws.relab[1].ensure((uint64_t)k * g->n * 4);
+            rows = g->ctx->ws.relab[1].as<uint32_t>();
+        }
+        if (k <= 64) {
+            if (o64) msbfs_impl<unsigned long long, 1>(g, h_srcs, k, rows, flags, rr);
+            else msbfs_impl<uint32_t, 1>(g, h_srcs, k, rows, flags, rr);
+        } else if (k <= 128) {
+            if (o64) msbfs_impl<unsigned long long, 2>(g, h_srcs, k, rows, flags, rr);
+            else msbfs_impl<uint32_t, 2>(g, h_srcs, k, rows, flags, rr);
+        } else {
+            if (o64) msbfs_impl<unsigned long long, 4>(g, h_srcs, k, rows, flags, rr);
+            else msbfs_impl<uint32_t, 4>(g, h_srcs, k, rows, flags, rr);
+        }
+        if (g->relabeled) unpermute_u32(g, rows, d_rows, k);
     }
     return true;
 }

@@ -485,14 +485,16 @@ __global__ void k_prk_init(const OffT *off, const uint32_t *src, float *c, doubl
     else c[(uint64_t)v * K + s] = 1.f / (float)deg;
 }
 
-// rank[v*K + s] -> out[s*n + v] for s < k (32 vertices x K sources per tile).
+// rank[x*K + s] -> out[s*n + v] for s < k (32 vertices x K sources per tile),
+// x = newid[v] on a regrouped graph (else v).
 template <int K>
-__global__ void __launch_bounds__(kBlock) k_prk_out(const float *rank, uint64_t n, uint32_t k, float *out) {
+__global__ void __launch_bounds__(kBlock) k_prk_out(const float *rank, uint64_t n, uint32_t k,
+                                                    const uint32_t *newid, float *out) {
     __shared__ float t[32][K + 1];
     for (uint64_t v0 = (uint64_t)blockIdx.x * 32; v0 < n; v0 += (uint64_t)gridDim.x * 32) {
         for (int i = threadIdx.x; i < 32 * K; i += kBlock) {
             int vv = i / K, s = i % K;
-            if (v0 + vv < n) t[vv][s] = rank[(v0 + vv) * K + s];
+            if (v0 + vv < n) t[vv][s] = rank[(newid ? (uint64_t)newid[v0 + vv] : v0 + vv) * K + s];
         }
         __syncthreads();
         for (int i = threadIdx.x; i < 32 * K; i += kBlock) {
@@ -688,6 +690,7 @@ void ppr_multi_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, float *d_r
     uint32_t lanes[K];
     for (int s = 0; s < K; s++) lanes[s] = (uint32_t)s < k ? h_srcs[s] : 0xFFFFFFFFu;
     PTG_CUDA_TRY(cudaMemcpyAsync(d_src, lanes, sizeof(lanes), cudaMemcpyHostToDevice, st));
+    map_sources_dev(g, d_src, K);
     PTG_CUDA_TRY(cudaMemsetAsync(c[0], 0, n * K * 4, st));
     const OffT *off = g->d_off.as<OffT>();
     launch(ctx, "k_prk_init", k_prk_init<OffT, K>, 1, 32, 0, st, off, (const uint32_t *)d_src, c[0], dang);
@@ -734,7 +737,7 @@ void ppr_multi_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, float *d_r
         rr.edges_relaxed += g->m;
     }
     launch(ctx, "k_prk_out", k_prk_out<K>, grid_for((n + 31) / 32, 1, sms * 8), kBlock, 0, st,
-           (const float *)c[iters & 1], n, k, d_rows);
+           (const float *)c[iters & 1], n, k, (const uint32_t *)(g->relabeled ? g->d_newid.p : nullptr), d_rows);
     PTG_CUDA_TRY(cudaGetLastError());
     rr.iterations += iters;
 }
@@ -770,8 +773,16 @@ void run_pagerank(ptg_graph *g, bool personalized, uint32_t src, double damping,
     PTG_REQUIRE(!g->out_of_core, PTG_ERR_UNSUPPORTED, "PageRank needs the graph resident in HBM");
     PTG_REQUIRE(g->symmetric, PTG_ERR_UNSUPPORTED,
                 "pull PageRank needs a symmetric CSR (PTG_CSR_SYMMETRIC)");
-    if (g->off64) pagerank_impl<unsigned long long>(g, personalized, src, damping, iters, d_rank, rr);
-    else pagerank_impl<uint32_t>(g, personalized, src, damping, iters, d_rank, rr);
+    float *rank = d_rank;
+    if (g->relabeled) {
+        // ranks in the stored vertex order, mapped to caller ids after
+        if (personalized) src = map_source_host(g, src);
+        g->ctx->ws.relab[0].ensure(g->n * 4);
+        rank = g->ctx->ws.relab[0].as<float>();
+    }
+    if (g->off64) pagerank_impl<unsigned long long>(g, personalized, src, damping, iters, rank, rr);
+    else pagerank_impl<uint32_t>(g, personalized, src, damping, iters, rank, rr);
+    if (g->relabeled) unpermute_f32(g, rank, d_rank);
 }
 
 }  // namespace ptg

@@ -207,6 +207,7 @@ struct Prof {
 struct Workspace {
     DevBuf value, q[2], bm[2], farbm, vis, scan, rowstart, tiles, bsum, ctl, aux, aux2, flags;
     DevBuf ms[3];  // multi-source 64-bit masks
+    DevBuf relab[2];  // results in the stored vertex order, before mapping to caller ids
     PinnedBuf h_ctl, h_flags;
 };
 
@@ -258,6 +259,10 @@ struct ptg_graph {
     uint64_t n_pr_mid = 0, n_pr_big = 0, n_pr_items = 0, n_pr_longs = 0;
     bool pr_bins_built = false;
     uint32_t pr_mid = 0, pr_chunk = 0;  // the thresholds the bins were built with
+    // degree-grouped vertex order (resident symmetric graphs): the arrays
+    // above hold new ids; d_perm maps new -> caller id, d_newid caller -> new
+    bool relabeled = false;
+    ptg::DevBuf d_perm, d_newid;
     // out-of-core
     bool out_of_core = false;
     uint64_t resident_edges = 0;
@@ -323,5 +328,15 @@ int sm_count_of(ptg_ctx *ctx);
 // Builds a resident symmetric graph's PageRank degree bins now rather than on
 // first use.
 void pr_prepare_graph(ptg_graph *g);
+
+// Vertex order (relabel.cu).  relabel_graph regroups a resident symmetric
+// graph's vertices by degree when the context's tuning asks for it (returns
+// whether it did); the helpers map sources in and results out.
+bool relabel_graph(ptg_graph *g);
+void map_sources_dev(ptg_graph *g, uint32_t *d_ids, uint32_t k);
+uint32_t map_source_host(ptg_graph *g, uint32_t src);
+void unpermute_u32(ptg_graph *g, const uint32_t *tmp, uint32_t *out, uint32_t rows);
+void unpermute_f32(ptg_graph *g, const float *tmp, float *out);
+void cc_labels_out(ptg_graph *g, const uint32_t *lab, uint32_t *scratch, uint32_t *out);
 
 }  // namespace ptg

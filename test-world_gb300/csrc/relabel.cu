@@ -1,0 +1,336 @@
+// relabel.cu - degree-grouped vertex order for resident symmetric graphs.
+//
+// The reference keeps the caller's vertex ids (ptGraph/main.cu:97-121 reads
+// the CSR as given).  On a GB300 the random gathers of PageRank, the frontier
+// bitmap probes of bottom-up BFS and the atomics of SSSP/CC hit L1/L2 far more
+// often when the high-degree vertices - the endpoints of most edges - sit
+// together.  So a resident symmetric graph is stored with its vertices
+// grouped by floor(log2(degree)), highest group first, the caller's order kept
+// inside each group, and every row's neighbours in the caller's order (ids
+// mapped).  Every entry point maps sources in and results out, so callers see
+// their own ids; BFS levels, SSSP distances and CC labels are unchanged bit
+// for bit (CC labels are mapped back to the minimum caller id of each
+// component), PageRank only changes its per-row summation order.
+//
+// Build: two counting passes over contiguous vertex ranges (one warp each)
+// give a stable bucket order (perm: new -> caller id, newid: caller -> new);
+// a range scan gives the new offsets; rows are copied with mapped ids, long
+// rows by whole CTAs.
+#include <algorithm>
+#include <vector>
+
+#include "ptg_device.cuh"
+
+namespace ptg {
+namespace {
+
+constexpr int kVB = 33;            // vertex groups: 0..31 by degree, 32 = isolated
+constexpr uint32_t kLongGroup = 19;  // groups 0..19 hold the rows of >= 4096 edges
+
+__device__ __forceinline__ uint32_t vgroup(uint64_t deg) {
+    if (deg == 0) return 32u;
+    uint32_t lg = 63u - (uint32_t)__clzll((long long)deg);  // floor(log2 deg)
+    return lg >= 31u ? 0u : 31u - lg;
+}
+
+// per-range group counts, counts[k * nb + range]
+template <class OffT>
+__global__ void k_vg_count(const OffT *off, uint64_t n, uint64_t per, uint32_t nb, uint32_t *counts) {
+    __shared__ uint32_t c[kVB];
+    const unsigned lane = lane_id();
+    for (int k = lane; k < kVB; k += 32) c[k] = 0;
+    __syncwarp();
+    uint64_t v0 = blockIdx.x * per, v1 = min(n, v0 + per);
+    for (uint64_t c0 = v0; c0 < v1; c0 += 32) {
+        uint64_t v = c0 + lane;
+        bool valid = v < v1;
+        uint32_t key = valid ? vgroup((uint64_t)(off[v + 1] - off[v])) : 0xFFFFFFFFu;
+        unsigned mask = __match_any_sync(0xffffffffu, key);
+        if (valid && lane == (unsigned)(__ffs(mask) - 1)) c[key] += __popc(mask);
+        __syncwarp();
+    }
+    for (int k = lane; k < kVB; k += 32) counts[(uint64_t)k * nb + blockIdx.x] = c[k];
+}
+
+// stable placement: within a range in vertex order, ranges in order
+template <class OffT>
+__global__ void k_vg_fill(const OffT *off, uint64_t n, uint64_t per, uint32_t nb, const uint32_t *base,
+                          uint32_t *perm, uint32_t *newid) {
+    __shared__ uint32_t run[kVB];
+    const unsigned lane = lane_id();
+    for (int k = lane; k < kVB; k += 32) run[k] = base[(uint64_t)k * nb + blockIdx.x];
+    __syncwarp();
+    uint64_t v0 = blockIdx.x * per, v1 = min(n, v0 + per);
+    for (uint64_t c0 = v0; c0 < v1; c0 += 32) {
+        uint64_t v = c0 + lane;
+        bool valid = v < v1;
+        uint32_t key = valid ? vgroup((uint64_t)(off[v + 1] - off[v])) : 0xFFFFFFFFu;
+        unsigned mask = __match_any_sync(0xffffffffu, key);
+        if (valid) {
+            uint32_t pos = run[key] + __popc(mask & lanemask_lt());
+            perm[pos] = (uint32_t)v;
+            newid[v] = pos;
+        }
+        __syncwarp();
+        if (valid && lane == (unsigned)(__ffs(mask) - 1)) run[key] += __popc(mask);
+        __syncwarp();
+    }
+}
+
+// edges of each range of new rows
+template <class OffT>
+__global__ void k_nd_sum(const OffT *off, const uint32_t *perm, uint64_t n, uint64_t per,
+                         unsigned long long *sums) {
+    const unsigned lane = lane_id();
+    uint64_t r0 = blockIdx.x * per, r1 = min(n, r0 + per);
+    unsigned long long s = 0;
+    for (uint64_t r = r0 + lane; r < r1; r += 32) {
+        uint32_t u = perm[r];
+        s += (unsigned long long)(off[(uint64_t)u + 1] - off[u]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) sums[blockIdx.x] = s;
+}
+
+template <class OffT>
+__global__ void k_nd_fill(const OffT *off, const uint32_t *perm, uint64_t n, uint64_t per,
+                          const unsigned long long *base, OffT *noff) {
+    const unsigned lane = lane_id();
+    uint64_t r0 = blockIdx.x * per, r1 = min(n, r0 + per);
+    unsigned long long run = base[blockIdx.x];
+    for (uint64_t c0 = r0; c0 < r1; c0 += 32) {
+        uint64_t r = c0 + lane;
+        unsigned long long d = 0;
+        if (r < r1) {
+            uint32_t u = perm[r];
+            d = (unsigned long long)(off[(uint64_t)u + 1] - off[u]);
+        }
+        unsigned long long incl = d;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned long long y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (unsigned)o) incl += y;
+        }
+        if (r < r1) noff[r] = (OffT)(run + incl - d);
+        run += __shfl_sync(0xffffffffu, incl, 31);
+    }
+}
+
+// rows below the long groups: 8 lanes per row
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_relabel_rows(const OffT *off, const uint32_t *col, const uint32_t *w,
+                                                         const OffT *noff, const uint32_t *perm,
+                                                         const uint32_t *newid, uint64_t r_begin, uint64_t n,
+                                                         uint32_t *ncol, uint32_t *nw) {
+    const unsigned sub = threadIdx.x & 7u;
+    const uint64_t groups = (uint64_t)gridDim.x * blockDim.x / 8;
+    for (uint64_t r = r_begin + (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 8; r < n; r += groups) {
+        uint32_t u = perm[r];
+        OffT b = off[u], e = off[(uint64_t)u + 1];
+        OffT d = noff[r];
+        for (OffT i = sub; i < e - b; i += 8) {
+            ncol[d + i] = newid[col[b + i]];
+            if (w) nw[d + i] = w[b + i];
+        }
+    }
+}
+
+// rows of the long groups: one CTA per row
+template <class OffT>
+__global__ void __launch_bounds__(kBlock) k_relabel_long(const OffT *off, const uint32_t *col, const uint32_t *w,
+                                                         const OffT *noff, const uint32_t *perm,
+                                                         const uint32_t *newid, uint32_t *ncol, uint32_t *nw) {
+    uint64_t r = blockIdx.x;
+    uint32_t u = perm[r];
+    OffT b = off[u], e = off[(uint64_t)u + 1];
+    OffT d = noff[r];
+    OffT deg = e - b;
+    OffT i = threadIdx.x;
+    for (; i + 3 * kBlock < deg; i += 4 * kBlock) {
+        uint32_t c0 = col[b + i], c1 = col[b + i + kBlock], c2 = col[b + i + 2 * kBlock], c3 = col[b + i + 3 * kBlock];
+        ncol[d + i] = newid[c0];
+        ncol[d + i + kBlock] = newid[c1];
+        ncol[d + i + 2 * kBlock] = newid[c2];
+        ncol[d + i + 3 * kBlock] = newid[c3];
+        if (w) {
+            nw[d + i] = w[b + i];
+            nw[d + i + kBlock] = w[b + i + kBlock];
+            nw[d + i + 2 * kBlock] = w[b + i + 2 * kBlock];
+            nw[d + i + 3 * kBlock] = w[b + i + 3 * kBlock];
+        }
+    }
+    for (; i < deg; i += kBlock) {
+        ncol[d + i] = newid[col[b + i]];
+        if (w) nw[d + i] = w[b + i];
+    }
+}
+
+__global__ void k_map_ids(uint32_t *ids, uint32_t k, const uint32_t *newid) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < k && ids[i] != 0xFFFFFFFFu) ids[i] = newid[ids[i]];
+}
+
+// out[r * n + v] = tmp[r * n + newid[v]] for rows r < k (caller order out;
+// gathering measured faster than scattering through perm)
+template <class T>
+__global__ void __launch_bounds__(kBlock) k_unpermute(const T *tmp, const uint32_t *newid, uint64_t n, uint32_t k,
+                                                      T *out) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t x = newid[v];
+        for (uint32_t r = 0; r < k; r++) out[(uint64_t)r * n + v] = tmp[(uint64_t)r * n + x];
+    }
+}
+
+// component label (a new id shared by the component) -> minimum caller id.
+// The read before the atomic keeps the giant component's vertices from all
+// hitting one address: once its minimum is in, they see it and skip.
+__global__ void __launch_bounds__(kBlock) k_cc_minold(const uint32_t *lab, const uint32_t *perm, uint64_t n,
+                                                      uint32_t *minold) {
+    for (uint64_t x = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; x < n; x += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t l = lab[x], o = perm[x];
+        if (o < *(volatile const uint32_t *)&minold[l]) atomicMin(&minold[l], o);
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_cc_out(const uint32_t *lab, const uint32_t *perm, const uint32_t *minold,
+                                                   uint64_t n, uint32_t *out) {
+    for (uint64_t x = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; x < n; x += (uint64_t)gridDim.x * blockDim.x)
+        out[perm[x]] = minold[lab[x]];
+}
+
+inline void swap_buf(DevBuf &a, DevBuf &b) {
+    std::swap(a.p, b.p);
+    std::swap(a.bytes, b.bytes);
+}
+
+template <class OffT>
+void relabel_impl(ptg_graph *g) {
+    ptg_ctx *ctx = g->ctx;
+    cudaStream_t st = ctx->stream;
+    const uint64_t n = g->n, m = g->m;
+    const int sms = ctx->sm_count;
+    const OffT *off = g->d_off.as<OffT>();
+    DevBuf perm, newid;
+    perm.ensure(n * 4);
+    newid.ensure(n * 4);
+    // vertex groups over contiguous ranges of about 4096 vertices
+    const uint32_t nb = (uint32_t)std::min<uint64_t>(65535, std::max<uint64_t>(1, (n + 4095) / 4096));
+    const uint64_t per = (n + nb - 1) / nb;
+    DevBuf cnt;
+    cnt.ensure((uint64_t)kVB * nb * 4);
+    launch(ctx, "k_vg_count", k_vg_count<OffT>, nb, 32, 0, st, off, n, per, nb, cnt.as<uint32_t>());
+    std::vector<uint32_t> h((size_t)kVB * nb);
+    PTG_CUDA_TRY(cudaMemcpyAsync(h.data(), cnt.p, h.size() * 4, cudaMemcpyDeviceToHost, st));
+    PTG_CUDA_TRY(cudaStreamSynchronize(st));
+    uint64_t acc = 0;
+    std::vector<uint64_t> gstart(kVB + 1);
+    for (int k = 0; k < kVB; k++) {
+        gstart[k] = acc;
+        for (uint32_t b = 0; b < nb; b++) {
+            uint32_t x = h[(size_t)k * nb + b];
+            h[(size_t)k * nb + b] = (uint32_t)acc;
+            acc += x;
+        }
+    }
+    gstart[kVB] = acc;
+    PTG_REQUIRE(acc == n, PTG_ERR_CUDA, "vertex grouping lost vertices");
+    PTG_CUDA_TRY(cudaMemcpyAsync(cnt.p, h.data(), h.size() * 4, cudaMemcpyHostToDevice, st));
+    launch(ctx, "k_vg_fill", k_vg_fill<OffT>, nb, 32, 0, st, off, n, per, nb, (const uint32_t *)cnt.p,
+           perm.as<uint32_t>(), newid.as<uint32_t>());
+    // new offsets
+    DevBuf sums, noff;
+    sums.ensure((uint64_t)nb * 8);
+    launch(ctx, "k_nd_sum", k_nd_sum<OffT>, nb, 32, 0, st, off, (const uint32_t *)perm.p, n, per,
+           sums.as<unsigned long long>());
+    std::vector<unsigned long long> hs(nb);
+    PTG_CUDA_TRY(cudaMemcpyAsync(hs.data(), sums.p, nb * 8, cudaMemcpyDeviceToHost, st));
+    PTG_CUDA_TRY(cudaStreamSynchronize(st));
+    unsigned long long tot = 0;
+    for (uint32_t b = 0; b < nb; b++) {
+        unsigned long long x = hs[b];
+        hs[b] = tot;
+        tot += x;
+    }
+    PTG_REQUIRE(tot == m, PTG_ERR_CUDA, "regrouped offsets lost edges");
+    PTG_CUDA_TRY(cudaMemcpyAsync(sums.p, hs.data(), nb * 8, cudaMemcpyHostToDevice, st));
+    noff.ensure((n + 1) * sizeof(OffT));
+    launch(ctx, "k_nd_fill", k_nd_fill<OffT>, nb, 32, 0, st, off, (const uint32_t *)perm.p, n, per,
+           (const unsigned long long *)sums.p, noff.as<OffT>());
+    OffT mm = (OffT)m;
+    PTG_CUDA_TRY(cudaMemcpyAsync(noff.as<OffT>() + n, &mm, sizeof(OffT), cudaMemcpyHostToDevice, st));
+    // rows
+    DevBuf ncol, nw;
+    ncol.ensure(std::max<uint64_t>(m, 1) * 4);
+    if (g->weighted) nw.ensure(std::max<uint64_t>(m, 1) * 4);
+    const uint64_t nlong = gstart[kLongGroup + 1];
+    const uint32_t *w = g->weighted ? g->d_w.as<uint32_t>() : nullptr;
+    if (nlong)
+        launch(ctx, "k_relabel_long", k_relabel_long<OffT>, (unsigned)nlong, kBlock, 0, st, off,
+               (const uint32_t *)g->d_col.p, w, (const OffT *)noff.p, (const uint32_t *)perm.p,
+               (const uint32_t *)newid.p, ncol.as<uint32_t>(), g->weighted ? nw.as<uint32_t>() : nullptr);
+    if (nlong < n)
+        launch(ctx, "k_relabel_rows", k_relabel_rows<OffT>, grid_for((n - nlong) * 8, kBlock, sms * 8), kBlock, 0,
+               st, off, (const uint32_t *)g->d_col.p, w, (const OffT *)noff.p, (const uint32_t *)perm.p,
+               (const uint32_t *)newid.p, (uint64_t)nlong, n, ncol.as<uint32_t>(),
+               g->weighted ? nw.as<uint32_t>() : nullptr);
+    PTG_CUDA_TRY(cudaGetLastError());
+    PTG_CUDA_TRY(cudaStreamSynchronize(st));
+    swap_buf(g->d_off, noff);
+    swap_buf(g->d_col, ncol);
+    if (g->weighted) swap_buf(g->d_w, nw);
+    swap_buf(g->d_perm, perm);
+    swap_buf(g->d_newid, newid);
+    g->relabeled = true;
+    g->device_bytes += n * 8;
+}
+
+}  // namespace
+
+bool relabel_graph(ptg_graph *g) {
+    if (g->out_of_core || !g->symmetric || g->m == 0 || g->ctx->tuning.vertex_order == 0) return false;
+    // the rebuild holds both copies of the edge arrays for a moment
+    size_t dfree = 0, dtot = 0;
+    PTG_CUDA_TRY(cudaMemGetInfo(&dfree, &dtot));
+    uint64_t need = (g->n + 1) * (g->off64 ? 8 : 4) + g->m * (g->weighted ? 8 : 4) + g->n * 8 + (256ull << 20);
+    if (need > dfree) return false;
+    if (g->off64) relabel_impl<unsigned long long>(g);
+    else relabel_impl<uint32_t>(g);
+    return true;
+}
+
+void map_sources_dev(ptg_graph *g, uint32_t *d_ids, uint32_t k) {
+    if (!g->relabeled || k == 0) return;
+    launch(g->ctx, "k_map_ids", k_map_ids, (k + 255) / 256, 256, 0, g->ctx->stream, d_ids, k,
+           (const uint32_t *)g->d_newid.p);
+}
+
+uint32_t map_source_host(ptg_graph *g, uint32_t src) {
+    if (!g->relabeled) return src;
+    uint32_t x = 0;
+    PTG_CUDA_TRY(cudaMemcpyAsync(&x, g->d_newid.as<uint32_t>() + src, 4, cudaMemcpyDeviceToHost, g->ctx->stream));
+    PTG_CUDA_TRY(cudaStreamSynchronize(g->ctx->stream));
+    return x;
+}
+
+void unpermute_u32(ptg_graph *g, const uint32_t *tmp, uint32_t *out, uint32_t rows) {
+    launch(g->ctx, "k_unpermute_u32", k_unpermute<uint32_t>, grid_for(g->n, kBlock, g->ctx->sm_count * 8), kBlock, 0,
+           g->ctx->stream, tmp, (const uint32_t *)g->d_newid.p, g->n, rows, out);
+}
+
+void unpermute_f32(ptg_graph *g, const float *tmp, float *out) {
+    launch(g->ctx, "k_unpermute_f32", k_unpermute<float>, grid_for(g->n, kBlock, g->ctx->sm_count * 8), kBlock, 0,
+           g->ctx->stream, tmp, (const uint32_t *)g->d_newid.p, g->n, 1u, out);
+}
+
+void cc_labels_out(ptg_graph *g, const uint32_t *lab, uint32_t *scratch, uint32_t *out) {
+    ptg_ctx *ctx = g->ctx;
+    cudaStream_t st = ctx->stream;
+    int grid = grid_for(g->n, kBlock, ctx->sm_count * 8);
+    PTG_CUDA_TRY(cudaMemsetAsync(scratch, 0xFF, g->n * 4, st));
+    launch(ctx, "k_cc_minold", k_cc_minold, grid, kBlock, 0, st, lab, (const uint32_t *)g->d_perm.p, g->n, scratch);
+    launch(ctx, "k_cc_out", k_cc_out, grid, kBlock, 0, st, lab, (const uint32_t *)g->d_perm.p,
+           (const uint32_t *)scratch, g->n, out);
+}
+
+}  // namespace ptg

@@ -125,6 +125,9 @@ ptg_graph *make_view(ptg_graph *g, ptg_ctx *lane) {
     alias(v->d_pr_longs, g->d_pr_longs);
     alias(v->d_nzbm, g->d_nzbm);
     alias(v->d_pull_items, g->d_pull_items);
+    alias(v->d_perm, g->d_perm);
+    alias(v->d_newid, g->d_newid);
+    v->relabeled = g->relabeled;
     v->n_pull_items = g->n_pull_items;
     v->pull_items_built = g->pull_items_built;
     v->pull_small = g->pull_small;
@@ -159,6 +162,8 @@ void drop_view(ptg_graph *v, const ptg_graph *g) {
     detach(v->d_pr_longs, g->d_pr_longs);
     detach(v->d_nzbm, g->d_nzbm);
     detach(v->d_pull_items, g->d_pull_items);
+    detach(v->d_perm, g->d_perm);
+    detach(v->d_newid, g->d_newid);
     delete v;
 }
 

@@ -71,9 +71,10 @@ __global__ void k_fill_bits(uint32_t *bm, uint64_t n) {
 }
 
 // Seed a single-source frontier.
-__global__ void k_seed(uint32_t *value, uint32_t src, uint32_t base, uint32_t *q, uint32_t *bm,
-                       uint32_t *vis, TravCtl *ctl) {
-    value[src] = base;
+__global__ void k_seed(uint32_t *value, uint32_t src, const uint32_t *newid, bool value_by_caller_id,
+                       uint32_t base, uint32_t *q, uint32_t *bm, uint32_t *vis, TravCtl *ctl) {
+    value[value_by_caller_id ? src : (newid ? newid[src] : src)] = base;
+    if (newid) src = newid[src];  // caller id -> stored vertex order
     q[0] = src;
     bm[src >> 5] |= 1u << (src & 31u);
     if (vis) vis[src >> 5] |= 1u << (src & 31u);
@@ -89,7 +90,14 @@ struct PushTargets {
     uint32_t *far_bm;  // near/far SSSP: vertices parked above the threshold (nullptr: none)
     uint32_t *vis;     // BFS: visited bitmap (nullptr otherwise)
     TravCtl *ctl;
+    // BFS on a degree-grouped graph: levels go straight to the caller's ids
+    // (value[perm[v]]); nullptr: value is indexed by stored id
+    const uint32_t *perm;
 };
+
+__device__ __forceinline__ uint32_t value_slot(const PushTargets &t, uint32_t v) {
+    return t.perm ? t.perm[v] : v;
+}
 
 // BFS relax: every target of a level gets the same value, so an unvisited
 // target is marked with a plain store of the level (racing stores write the
@@ -97,8 +105,11 @@ struct PushTargets {
 // scale 24, resident in L2) absorbs it when the frontier is compacted.
 __device__ __forceinline__ void relax_bfs(const PushTargets &t, uint32_t v, uint32_t nd) {
     uint32_t bit = 1u << (v & 31u);
-    if (t.vis[v >> 5] & bit) return;
-    t.value[v] = nd;
+    // a target already marked this level (a hub reached by many edges) takes
+    // no further store or reduction; both words are read in parallel
+    uint32_t seen = t.vis[v >> 5] | *(volatile const uint32_t *)&t.bm_next[v >> 5];
+    if (seen & bit) return;
+    t.value[value_slot(t, v)] = nd;
     atomicOr(&t.bm_next[v >> 5], bit);
 }
 
@@ -210,7 +221,7 @@ __global__ void __launch_bounds__(kBlock) k_expand(const uint32_t *q, const OffT
                 s_sc[k] = sc[r0 + k];
                 if (k < nrows) {
                     s_rs[k] = rs[r0 + k];
-                    s_val[k] = t.value[q[r0 + k]];
+                    s_val[k] = t.value[value_slot(t, q[r0 + k])];
                 }
             }
             __syncthreads();
@@ -262,7 +273,7 @@ __global__ void __launch_bounds__(kBlock) k_expand(const uint32_t *q, const OffT
             for (uint64_t j = t0 + threadIdx.x; j < t1; j += kBlock) {
                 uint64_t row = last_le(sc, r0, r0 + nrows, j);
                 uint64_t e = (uint64_t)rs[row] + (j - (uint64_t)sc[row]);
-                uint32_t uval = t.value[q[row]];
+                uint32_t uval = t.value[value_slot(t, q[row])];
                 uint32_t v = __ldcs(col + e);
                 if (MODE == 0 && t.vis) {
                     relax_bfs(t, v, uval + 1u);
@@ -366,7 +377,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_bottom_up(uint64_t n, const OffT 
             }
             if (found) {
                 atomicOr(&s_found[wid][(v >> 5) - (uint32_t)(c * kBuWords)], 1u << (v & 31u));
-                t.value[v] = newval;
+                t.value[value_slot(t, v)] = newval;
             }
         }
         __syncwarp();
@@ -598,6 +609,9 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
     const uint64_t n = g->n;
     const int sms = ctx->sm_count;
     const uint64_t words = (n + 31) / 32;
+    // BFS on a degree-grouped graph writes levels by caller id directly (it
+    // never compares them); the other traversals run on stored ids
+    const bool bfs_by_caller_id = kind == TRAV_BFS && g->relabeled;
 
     ws.q[0].ensure(n * 4);
     ws.q[1].ensure(n * 4);
@@ -666,7 +680,9 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
     }
     PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &init, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
     if (kind != TRAV_CCPROP)
-        launch(ctx, "k_seed", k_seed, 1, 1, 0, st, d_value, src, base, ws.q[0].as<uint32_t>(),
+        launch(ctx, "k_seed", k_seed, 1, 1, 0, st, d_value, src,
+               (const uint32_t *)(g->relabeled ? g->d_newid.p : nullptr), bfs_by_caller_id, base,
+               ws.q[0].as<uint32_t>(),
                ws.bm[0].as<uint32_t>(), vis, d_ctl);
     PTG_CUDA_TRY(cudaGetLastError());
 
@@ -730,7 +746,8 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         uint32_t *q_cur = ws.q[cur].as<uint32_t>(), *q_nxt = ws.q[cur ^ 1].as<uint32_t>();
         uint32_t *bm_cur = ws.bm[cur].as<uint32_t>(), *bm_nxt = ws.bm[cur ^ 1].as<uint32_t>();
         PTG_CUDA_TRY(cudaMemsetAsync(bm_nxt, 0, words * 4, st));
-        PushTargets pt{d_value, bm_nxt, use_far ? ws.farbm.as<uint32_t>() : nullptr, vis, d_ctl};
+        PushTargets pt{d_value, bm_nxt, use_far ? ws.farbm.as<uint32_t>() : nullptr, vis, d_ctl,
+                       bfs_by_caller_id ? g->d_perm.as<uint32_t>() : nullptr};
         int scan_blocks = grid_for(F, kBlock, kScanBlocks);
         unsigned long long *bsum = ws.bsum.as<unsigned long long>();
         OffT *sc = ws.scan.as<OffT>(), *rs = ws.rowstart.as<OffT>();
@@ -917,8 +934,23 @@ void trav_prepare_graph(ptg_graph *g) {
 
 void run_traversal(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value, uint32_t flags,
                    uint32_t delta, uint32_t max_iters, RunResult &rr) {
-    if (g->off64) traverse_impl<unsigned long long>(g, kind, src, d_value, flags, delta, max_iters, rr);
-    else traverse_impl<uint32_t>(g, kind, src, d_value, flags, delta, max_iters, rr);
+    uint32_t *val = d_value;
+    Workspace &ws = g->ctx->ws;
+    if (g->relabeled && kind != TRAV_BFS) {
+        // run in the stored vertex order, then map the values to caller ids
+        ws.relab[0].ensure(g->n * 4);
+        val = ws.relab[0].as<uint32_t>();
+    }
+    if (g->off64) traverse_impl<unsigned long long>(g, kind, src, val, flags, delta, max_iters, rr);
+    else traverse_impl<uint32_t>(g, kind, src, val, flags, delta, max_iters, rr);
+    if (!g->relabeled || kind == TRAV_BFS) return;
+    if (kind == TRAV_CCPROP) {
+        ws.relab[1].ensure(g->n * 4);
+        cc_labels_out(g, val, ws.relab[1].as<uint32_t>(), d_value);
+    } else {
+        unpermute_u32(g, val, d_value, 1);
+    }
+    PTG_CUDA_TRY(cudaGetLastError());
 }
 
 }  // namespace ptg

@@ -10,6 +10,7 @@ Reference mapping (ptGraph/main.cu:24-56):
   ccCaculateIn{Opt,Share}                   -> Graph.cc
   prCaculateIn{Share,Opt} (a stub there)    -> Graph.pagerank
 """
+import atexit
 import ctypes
 import weakref
 import os
@@ -125,11 +126,12 @@ class Tuning(ctypes.Structure):
                 ("sssp_delta_scale", ctypes.c_float), ("expand_ctas_per_sm", ctypes.c_uint32),
                 ("pr_ctas_per_sm", ctypes.c_uint32), ("pr_mid", ctypes.c_uint32), ("pr_chunk", ctypes.c_uint32),
                 ("ms_pull_small", ctypes.c_uint32), ("ms_pull_chunk", ctypes.c_uint32),
-                ("reserved0", ctypes.c_uint32 * 2), ("partition_bytes", ctypes.c_uint64),
+                ("vertex_order", ctypes.c_uint32), ("reserved0", ctypes.c_uint32),
+                ("partition_bytes", ctypes.c_uint64),
                 ("reserved", ctypes.c_uint32 * 8)]
 
     KNOBS = ("bfs_alpha", "bfs_beta", "sssp_delta_scale", "expand_ctas_per_sm", "pr_ctas_per_sm", "pr_mid",
-             "pr_chunk", "ms_pull_small", "ms_pull_chunk", "partition_bytes")
+             "pr_chunk", "ms_pull_small", "ms_pull_chunk", "vertex_order", "partition_bytes")
 
     def as_dict(self):
         return {k: (round(float(getattr(self, k)), 6) if isinstance(getattr(self, k), float) else int(getattr(self, k)))
@@ -275,6 +277,21 @@ def partition_config(**kw):
     return cfg
 
 
+_LIVE_CTX = weakref.WeakSet()
+
+
+@atexit.register
+def _close_live_contexts():
+    """Close contexts still open at interpreter exit (servers, then graphs,
+    then the context), while the CUDA runtime and this module are intact;
+    module teardown would otherwise destroy them in arbitrary order."""
+    for c in list(_LIVE_CTX):
+        try:
+            c.close()
+        except Exception:
+            pass
+
+
 class Ctx:
     """A context on one CUDA device (owns streams and reusable workspace)."""
 
@@ -283,6 +300,7 @@ class Ctx:
         self.h = _vp()
         self._deps = weakref.WeakSet()  # graphs and servers, closed before the context
         _check(lib().ptg_ctx_create(device, ctypes.byref(self.h)))
+        _LIVE_CTX.add(self)
 
     def close(self):
         if self.h:

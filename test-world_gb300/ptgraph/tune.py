@@ -13,6 +13,8 @@ module picks them by measurement on the device it runs on:
   the PageRank SpMV (pr_ctas_per_sm);
 * schedule thresholds: the direction-optimizing BFS switch (bfs_alpha,
   bfs_beta) and the SSSP bucket width (sssp_delta_scale);
+* the stored vertex order of resident symmetric graphs (vertex_order: as
+  given, or grouped by degree);
 * partition size of out-of-core graphs (partition_bytes).
 
 Each knob is swept in turn over its candidates with the others at their best
@@ -51,6 +53,7 @@ CANDIDATES = {
     "sssp_delta_scale": [0.25, 0.5, 1.0, 2.0, 4.0, 8.0],
     "ms_pull_small": [8, 16, 32, 64, 128],
     "ms_pull_chunk": [256, 512, 1024, 2048, 4096],
+    "vertex_order": [0, 1],
     "partition_bytes": [8 << 20, 16 << 20, 32 << 20, 64 << 20, 128 << 20, 256 << 20, 512 << 20],
 }
 
@@ -58,7 +61,7 @@ CANDIDATES = {
 WORKLOAD = {
     "pr_mid": "pagerank", "pr_chunk": "pagerank", "pr_ctas_per_sm": "pagerank",
     "bfs_alpha": "bfs", "bfs_beta": "bfs", "expand_ctas_per_sm": "bfs_sssp",
-    "sssp_delta_scale": "sssp", "ms_pull_small": "msbfs", "ms_pull_chunk": "msbfs",
+    "sssp_delta_scale": "sssp", "ms_pull_small": "msbfs", "ms_pull_chunk": "msbfs", "vertex_order": "all",
     "partition_bytes": "ooc_sssp",
 }
 
@@ -134,6 +137,9 @@ class _Bench:
             out = self._dev((self.n_ms, n), torch.int32)
             G.msbfs(self.sources[:self.n_ms], stats=st, out=out, flags=dev)
             return st["device_ms"], out.cpu().numpy()
+        if kind == "all":
+            parts = [self.run(k) for k in ("pagerank", "bfs_sssp", "msbfs")]
+            return sum(p[0] for p in parts), [p[1] for p in parts]
         if kind == "ooc_sssp":
             if self._ooc is None:
                 self._ooc = ptgraph.gen_rmat(self.ooc_scale, 16, 0.57, 0.19, 0.19, seed=3, symmetric=False,
@@ -153,6 +159,8 @@ class _Bench:
 
 
 def _same(kind, a, b):
+    if kind == "all":
+        return all(_same(k, x, y) for k, x, y in zip(("pagerank", "bfs_sssp", "msbfs"), a, b))
     if kind == "pagerank":
         a = np.asarray(a, dtype=np.float64)
         b = np.asarray(b, dtype=np.float64)

@@ -16,14 +16,14 @@ PR_RTOL = 1e-6  # max per-vertex relative error vs the FP64 oracle
 # every knob away from its default (and inside its range)
 OFF_DEFAULT = {"bfs_alpha": 6.0, "bfs_beta": 36.0, "sssp_delta_scale": 2.0, "expand_ctas_per_sm": 3,
                "pr_ctas_per_sm": 5, "pr_mid": 16, "pr_chunk": 1024, "ms_pull_small": 8, "ms_pull_chunk": 256,
-               "partition_bytes": 1 << 20}
+               "vertex_order": 0, "partition_bytes": 1 << 20}
 
 
 def test_builtin_values(ptg):
     d = ptg.tuning_defaults()
     assert d == {"bfs_alpha": 15.0, "bfs_beta": 18.0, "sssp_delta_scale": 0.5, "expand_ctas_per_sm": 8,
                  "pr_ctas_per_sm": 8, "pr_mid": 64, "pr_chunk": 4096, "ms_pull_small": 32,
-                 "ms_pull_chunk": 1024, "partition_bytes": 256 << 20}
+                 "ms_pull_chunk": 1024, "vertex_order": 1, "partition_bytes": 256 << 20}
     assert ptg.tuning_valid(d)
     assert ptg.tuning_valid(OFF_DEFAULT)
 
@@ -33,7 +33,7 @@ def test_builtin_values(ptg):
     {"ms_pull_chunk": 100}, {"ms_pull_chunk": 16}, {"ms_pull_small": 0}, {"ms_pull_small": 5000},
     {"expand_ctas_per_sm": 0}, {"expand_ctas_per_sm": 33}, {"pr_ctas_per_sm": 0},
     {"bfs_alpha": 0.0}, {"bfs_alpha": math.nan}, {"bfs_beta": math.inf}, {"sssp_delta_scale": -1.0},
-    {"partition_bytes": 4096}, {"partition_bytes": 1 << 40},
+    {"partition_bytes": 4096}, {"partition_bytes": 1 << 40}, {"vertex_order": 2},
 ])
 def test_out_of_range_rejected(ptg, bad):
     assert not ptg.tuning_valid(bad)
@@ -126,10 +126,71 @@ def test_results_unchanged_under_other_knobs(ptg, oracle, tctx):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("case", ["rmat", "components"])
+def test_vertex_order_keeps_results(ptg, oracle, tctx, case):
+    """A degree-grouped graph answers in caller ids exactly as one stored as
+    given: levels, distances, CC labels (minimum caller id per component) and
+    multi-source rows bit for bit, PageRank within the tolerance."""
+    if case == "rmat":
+        off, col, w = ptg.gen_rmat(15, 16, seed=21, symmetric=True, wmin=1, wmax=63)
+    else:
+        # many small components, isolated vertices between them, hubs with long rows
+        rng = np.random.default_rng(5)
+        n = 30000
+        edges = set()
+        for c0 in range(0, n - 50, 97):
+            k = int(rng.integers(2, 40))
+            for _ in range(k * 2):
+                a, b = (int(x) for x in rng.integers(c0, c0 + k, 2))
+                if a != b:
+                    edges.add((a, b))
+                    edges.add((b, a))
+        for v in range(1, 6000):
+            edges.add((29990, v * 3 % 29000))
+            edges.add((v * 3 % 29000, 29990))
+        e = np.array(sorted(edges), dtype=np.int64)
+        e = e[e[:, 0] != e[:, 1]]
+        off = np.zeros(n + 1, dtype=np.uint64)
+        np.add.at(off, e[:, 0] + 1, 1)
+        off = np.cumsum(off).astype(np.uint64)
+        col = e[:, 1].astype(np.uint32)
+        w = rng.integers(1, 64, col.size).astype(np.uint32)
+    deg = np.diff(off.astype(np.int64))
+    srcs = np.random.default_rng(9).choice(np.nonzero(deg)[0], 5, replace=False).astype(np.uint32)
+    res = {}
+    for order in (0, 1):
+        tctx.set_tuning(vertex_order=order)
+        G = tctx.graph(off, col, w, symmetric=True)
+        r = {"bfs": [G.bfs(int(s)) for s in srcs], "sssp": [G.sssp(int(s)) for s in srcs], "cc": G.cc(),
+             "ccref": G.cc(flags=ptg.PTG_REFERENCE_SCHEDULE), "pr": G.pagerank(),
+             "ppr": [G.ppr(int(s)) for s in srcs], "pprb": G.ppr_batch(srcs), "msb": G.msbfs(srcs),
+             "mss": G.mssssp(srcs)}
+        res[order] = r
+        G.close()
+    tctx.set_tuning()
+    a, b = res[0], res[1]
+    for i, s in enumerate(srcs):
+        ref_b = oracle.bfs(off, col, int(s), method="queue")
+        ref_s = oracle.sssp(off, col, w, int(s))
+        assert (a["bfs"][i] == ref_b).all() and (b["bfs"][i] == ref_b).all()
+        assert (a["sssp"][i] == ref_s).all() and (b["sssp"][i] == ref_s).all()
+        assert (b["msb"][i] == ref_b).all() and (b["mss"][i] == ref_s).all()
+        assert np.array_equal(b["pprb"][i], b["ppr"][i])
+        pref = oracle.ppr(off, col, int(s))
+        nz = pref > 1e-30
+        assert (np.abs(b["ppr"][i][nz] - pref[nz]) / pref[nz]).max() < PR_RTOL
+    ref_cc = oracle.cc(off, col, method="unionfind")
+    for order in (0, 1):
+        assert (res[order]["cc"] == ref_cc).all() and (res[order]["ccref"] == ref_cc).all()
+    pr_ref = oracle.pagerank(off, col)
+    assert (np.abs(b["pr"].astype(np.float64) - pr_ref) / pr_ref).max() < PR_RTOL
+
+
+@pytest.mark.gpu
 def test_autotuner_small_run(ptg, tctx, tmp_path):
     from ptgraph import tune
     knobs = ["pr_mid", "bfs_alpha", "expand_ctas_per_sm", "sssp_delta_scale", "ms_pull_small",
-             "partition_bytes"]
+             "vertex_order", "partition_bytes"]
     doc = tune.tune(tctx, scale=13, repeats=1, knobs=knobs, n_bfs=4, n_sssp=2, n_ms=16, ooc_scale=15,
                     log=lambda *a: None)
     assert set(doc["sweeps"]) == set(knobs)
