@@ -6,16 +6,17 @@
 // often when the high-degree vertices - the endpoints of most edges - sit
 // together.  So a resident symmetric graph is stored with its vertices
 // grouped by floor(log2(degree)), highest group first, the caller's order kept
-// inside each group, and every row's neighbours in the caller's order (ids
-// mapped).  Every entry point maps sources in and results out, so callers see
+// inside each group, and every row's neighbours (ids mapped) ordered so that
+// high-degree neighbours come first.  Every entry point maps sources in and results out, so callers see
 // their own ids; BFS levels, SSSP distances and CC labels are unchanged bit
 // for bit (CC labels are mapped back to the minimum caller id of each
 // component), PageRank only changes its per-row summation order.
 //
 // Build: two counting passes over contiguous vertex ranges (one warp each)
 // give a stable bucket order (perm: new -> caller id, newid: caller -> new);
-// a range scan gives the new offsets; rows are copied with mapped ids, long
-// rows by whole CTAs.
+// a range scan gives the new offsets; rows are copied with mapped ids (short
+// and medium rows reordered by neighbour group, rows of 4096+ edges by whole
+// CTAs in the caller's order).
 #include <algorithm>
 #include <vector>
 
@@ -117,21 +118,120 @@ __global__ void k_nd_fill(const OffT *off, const uint32_t *perm, uint64_t n, uin
     }
 }
 
-// rows below the long groups: 8 lanes per row
+// Rows below the long groups, a warp per 32 consecutive new rows.  Each row
+// is written with its neighbours' new ids so that the high-degree neighbours
+// come first (bottom-up BFS stops at the first frontier neighbour, and those
+// are mostly hubs): rows of up to 16 edges are sorted by new id in registers
+// (one lane each); longer rows are split stably by neighbour group (a warp
+// each), which also leaves them sorted by new id when the caller's rows were
+// sorted by id.
+constexpr int kSmallRow = 16;
+
+__device__ __forceinline__ uint32_t group_of(const uint32_t *gstart, uint32_t x) {
+    // largest k with gstart[k] <= x, k in 0..kVB-1 (gstart has kVB + 1 entries)
+    uint32_t lo = 0, hi = kVB;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (gstart[mid] <= x) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
 template <class OffT>
 __global__ void __launch_bounds__(kBlock) k_relabel_rows(const OffT *off, const uint32_t *col, const uint32_t *w,
                                                          const OffT *noff, const uint32_t *perm,
-                                                         const uint32_t *newid, uint64_t r_begin, uint64_t n,
-                                                         uint32_t *ncol, uint32_t *nw) {
-    const unsigned sub = threadIdx.x & 7u;
-    const uint64_t groups = (uint64_t)gridDim.x * blockDim.x / 8;
-    for (uint64_t r = r_begin + (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 8; r < n; r += groups) {
-        uint32_t u = perm[r];
-        OffT b = off[u], e = off[(uint64_t)u + 1];
-        OffT d = noff[r];
-        for (OffT i = sub; i < e - b; i += 8) {
-            ncol[d + i] = newid[col[b + i]];
-            if (w) nw[d + i] = w[b + i];
+                                                         const uint32_t *newid, const uint32_t *gstart_g,
+                                                         uint64_t r_begin, uint64_t n, uint32_t *ncol,
+                                                         uint32_t *nw) {
+    __shared__ uint32_t gstart[kVB + 1];
+    __shared__ uint32_t cnt[kBlock / 32][32];
+    for (int i = threadIdx.x; i <= kVB; i += kBlock) gstart[i] = gstart_g[i];
+    __syncthreads();
+    const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
+    const uint64_t ntiles = (n - r_begin + 31) / 32;
+    const uint64_t nwarps = (uint64_t)gridDim.x * (kBlock / 32);
+    for (uint64_t tile = blockIdx.x * (uint64_t)(kBlock / 32) + wid; tile < ntiles; tile += nwarps) {
+        uint64_t r = r_begin + tile * 32 + lane;
+        bool valid = r < n;
+        uint32_t u = valid ? perm[r] : 0u;
+        OffT b = valid ? off[u] : (OffT)0;
+        OffT deg = valid ? (OffT)(off[(uint64_t)u + 1] - b) : (OffT)0;
+        OffT d = valid ? noff[r] : (OffT)0;
+        if (deg > 0 && deg <= (OffT)kSmallRow) {
+            uint32_t key[kSmallRow], wv[kSmallRow];
+#pragma unroll
+            for (int i = 0; i < kSmallRow; i++) {
+                key[i] = (OffT)i < deg ? newid[col[b + i]] : 0xFFFFFFFFu;
+                wv[i] = (w && (OffT)i < deg) ? w[b + i] : 0u;
+            }
+            // bitonic network on 16 (fixed compare-exchange order: deterministic)
+#pragma unroll
+            for (int k = 2; k <= kSmallRow; k <<= 1)
+#pragma unroll
+                for (int j = k >> 1; j > 0; j >>= 1)
+#pragma unroll
+                    for (int i = 0; i < kSmallRow; i++) {
+                        int l = i ^ j;
+                        if (l > i) {
+                            bool up = (i & k) == 0;
+                            if ((key[i] > key[l]) == up) {
+                                uint32_t t = key[i];
+                                key[i] = key[l];
+                                key[l] = t;
+                                t = wv[i];
+                                wv[i] = wv[l];
+                                wv[l] = t;
+                            }
+                        }
+                    }
+#pragma unroll
+            for (int i = 0; i < kSmallRow; i++)
+                if ((OffT)i < deg) {
+                    ncol[d + i] = key[i];
+                    if (w) nw[d + i] = wv[i];
+                }
+        }
+        unsigned big = __ballot_sync(0xffffffffu, deg > (OffT)kSmallRow);
+        while (big) {
+            int src = __ffs(big) - 1;
+            big &= big - 1;
+            OffT B = __shfl_sync(0xffffffffu, b, src), D = __shfl_sync(0xffffffffu, d, src);
+            OffT DEG = __shfl_sync(0xffffffffu, deg, src);
+            cnt[wid][lane] = 0;
+            __syncwarp();
+            for (OffT c0 = 0; c0 < DEG; c0 += 32) {  // pass 1: neighbours per group
+                OffT i = c0 + lane;
+                bool ok = i < DEG;
+                uint32_t key = ok ? min(group_of(gstart, newid[col[B + i]]), 31u) : 0xFFFFFFFFu;
+                unsigned mask = __match_any_sync(0xffffffffu, key);
+                if (ok && lane == (unsigned)(__ffs(mask) - 1)) cnt[wid][key] += __popc(mask);
+                __syncwarp();
+            }
+            uint32_t cv = cnt[wid][lane], incl = cv;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (unsigned)o) incl += y;
+            }
+            __syncwarp();
+            cnt[wid][lane] = incl - cv;  // first slot of each group
+            __syncwarp();
+            for (OffT c0 = 0; c0 < DEG; c0 += 32) {  // pass 2: stable placement
+                OffT i = c0 + lane;
+                bool ok = i < DEG;
+                uint32_t nid = ok ? newid[col[B + i]] : 0u;
+                uint32_t key = ok ? min(group_of(gstart, nid), 31u) : 0xFFFFFFFFu;
+                unsigned mask = __match_any_sync(0xffffffffu, key);
+                if (ok) {
+                    OffT pos = D + (OffT)(cnt[wid][key] + __popc(mask & lanemask_lt()));
+                    ncol[pos] = nid;
+                    if (w) nw[pos] = w[B + i];
+                }
+                __syncwarp();
+                if (ok && lane == (unsigned)(__ffs(mask) - 1)) cnt[wid][key] += __popc(mask);
+                __syncwarp();
+            }
         }
     }
 }
@@ -269,11 +369,17 @@ void relabel_impl(ptg_graph *g) {
         launch(ctx, "k_relabel_long", k_relabel_long<OffT>, (unsigned)nlong, kBlock, 0, st, off,
                (const uint32_t *)g->d_col.p, w, (const OffT *)noff.p, (const uint32_t *)perm.p,
                (const uint32_t *)newid.p, ncol.as<uint32_t>(), g->weighted ? nw.as<uint32_t>() : nullptr);
-    if (nlong < n)
-        launch(ctx, "k_relabel_rows", k_relabel_rows<OffT>, grid_for((n - nlong) * 8, kBlock, sms * 8), kBlock, 0,
-               st, off, (const uint32_t *)g->d_col.p, w, (const OffT *)noff.p, (const uint32_t *)perm.p,
-               (const uint32_t *)newid.p, (uint64_t)nlong, n, ncol.as<uint32_t>(),
+    std::vector<uint32_t> gs(kVB + 1);
+    DevBuf gsd;
+    if (nlong < n) {
+        for (int k = 0; k <= kVB; k++) gs[k] = (uint32_t)gstart[k];
+        gsd.ensure(gs.size() * 4);
+        PTG_CUDA_TRY(cudaMemcpyAsync(gsd.p, gs.data(), gs.size() * 4, cudaMemcpyHostToDevice, st));
+        launch(ctx, "k_relabel_rows", k_relabel_rows<OffT>, grid_for((n - nlong + 31) / 32, kBlock / 32, sms * 8),
+               kBlock, 0, st, off, (const uint32_t *)g->d_col.p, w, (const OffT *)noff.p, (const uint32_t *)perm.p,
+               (const uint32_t *)newid.p, (const uint32_t *)gsd.p, (uint64_t)nlong, n, ncol.as<uint32_t>(),
                g->weighted ? nw.as<uint32_t>() : nullptr);
+    }
     PTG_CUDA_TRY(cudaGetLastError());
     PTG_CUDA_TRY(cudaStreamSynchronize(st));
     swap_buf(g->d_off, noff);
