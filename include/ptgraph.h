@@ -123,7 +123,7 @@ enum {
 
 typedef struct ptg_partition_config {
     uint64_t partition_bytes;     /* edge bytes per streamed partition; 0 = the
-                                     context's tuning (256 MiB unless tuned)          */
+                                     context's tuning (32 MiB unless tuned)           */
     uint64_t device_budget_bytes; /* bytes of HBM for resident edges; 0 = use frac   */
     double device_frac;           /* fraction of free HBM for resident edges; 0 = 0.9 */
     uint32_t n_staging_buffers;   /* 2 or 3 (double/triple buffering); 0 = 2          */
@@ -221,23 +221,25 @@ typedef struct ptg_tuning {
     float bfs_beta;              /* ... and back to push when the frontier holds fewer
                                     than n / bfs_beta vertices (default 18)              */
     float sssp_delta_scale;      /* default SSSP bucket width = this x the mean edge
-                                    weight (default 0.5; 0: label-correcting rounds)     */
-    uint32_t expand_ctas_per_sm; /* push relax (k_expand) CTAs per SM, 1..32 (default 8) */
+                                    weight (default 2; 0: label-correcting rounds)       */
+    uint32_t expand_ctas_per_sm; /* push relax (k_expand) CTAs per SM, 1..32 (default 4) */
     uint32_t pr_ctas_per_sm;     /* PageRank SpMV CTAs per SM, 1..32 (default 8)         */
     uint32_t pr_mid;             /* PageRank rows of 5..pr_mid edges run 8 lanes per
-                                    row, longer ones a warp (default 64; 8..pr_chunk)    */
+                                    row, longer ones a warp (default 256; 8..pr_chunk)   */
     uint32_t pr_chunk;           /* rows over pr_chunk edges are cut into pr_chunk-edge
                                     pieces (default 4096; 128..65536)                    */
     uint32_t ms_pull_small;      /* multi-source pull: rows up to this many edges take
                                     a thread, longer ones warps (default 32; 1..4096)    */
     uint32_t ms_pull_chunk;      /* edges per warp item of a long row (default 1024;
                                     32..65536, a multiple of 32)                         */
-    uint32_t vertex_order;       /* 1: resident symmetric graphs are stored with their
-                                    vertices grouped by degree (ids are mapped in and
-                                    out; results are unchanged); 0: as given (default 1)*/
+    uint32_t vertex_order;       /* resident symmetric graphs stored with their vertices
+                                    grouped by degree (ids mapped in and out, results
+                                    unchanged): 0 never; 1 (default) graphs of 2^20+
+                                    edges whose degrees are skewed (a fifth of the
+                                    edges at vertices of 8x the mean degree); 2 always */
     uint32_t reserved0;          /* zero; keeps partition_bytes at byte offset 48       */
     uint64_t partition_bytes;    /* edge bytes per partition of an out-of-core graph
-                                    created without a partition size (default 256 MiB;
+                                    created without a partition size (default 32 MiB;
                                     1 MiB..16 GiB)                                       */
     uint32_t reserved[8];
 } ptg_tuning;

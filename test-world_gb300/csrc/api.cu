@@ -113,7 +113,7 @@ void plan(uint64_t n, uint64_t m, const uint64_t *off, uint64_t bpe, const ptg_p
     ptg_partition_config cfg;
     ptg_partition_config_default(&cfg);
     if (cfg_in) cfg = *cfg_in;
-    if (cfg.partition_bytes == 0) cfg.partition_bytes = 256ull << 20;
+    if (cfg.partition_bytes == 0) cfg.partition_bytes = 32ull << 20;
     if (cfg.n_staging_buffers == 0) cfg.n_staging_buffers = 2;
     if (cfg.device_frac <= 0) cfg.device_frac = 0.9;
     PE = std::max<uint64_t>(1, cfg.partition_bytes / bpe);
@@ -209,7 +209,7 @@ const char *ptg_status_string(ptg_status s) {
 void ptg_partition_config_default(ptg_partition_config *cfg) {
     if (!cfg) return;
     std::memset(cfg, 0, sizeof(*cfg));
-    cfg->partition_bytes = 0;  // the context's tuned size (256 MiB for the host-only planner)
+    cfg->partition_bytes = 0;  // the context's tuned size (32 MiB for the host-only planner)
     cfg->device_budget_bytes = 0;
     cfg->device_frac = 0.9;
     cfg->n_staging_buffers = 2;
@@ -241,15 +241,15 @@ void ptg_tuning_defaults(ptg_tuning *t) {
     t->version = PTG_TUNING_VERSION;
     t->bfs_alpha = 15.f;
     t->bfs_beta = 18.f;
-    t->sssp_delta_scale = 0.5f;
-    t->expand_ctas_per_sm = 8;
+    t->sssp_delta_scale = 2.0f;
+    t->expand_ctas_per_sm = 4;
     t->pr_ctas_per_sm = 8;
-    t->pr_mid = 64;
+    t->pr_mid = 256;
     t->pr_chunk = 4096;
     t->ms_pull_small = 32;
     t->ms_pull_chunk = 1024;
     t->vertex_order = 1;
-    t->partition_bytes = 256ull << 20;
+    t->partition_bytes = 32ull << 20;
 }
 
 ptg_status ptg_tuning_validate(const ptg_tuning *t) {
@@ -263,7 +263,7 @@ ptg_status ptg_tuning_validate(const ptg_tuning *t) {
     if (t->pr_mid < 8 || t->pr_mid > t->pr_chunk) return PTG_ERR_INVALID;
     if (t->ms_pull_small < 1 || t->ms_pull_small > 4096) return PTG_ERR_INVALID;
     if (t->ms_pull_chunk < 32 || t->ms_pull_chunk > 65536 || t->ms_pull_chunk % 32) return PTG_ERR_INVALID;
-    if (t->vertex_order > 1) return PTG_ERR_INVALID;
+    if (t->vertex_order > 2) return PTG_ERR_INVALID;
     if (t->partition_bytes < (1ull << 20) || t->partition_bytes > (16ull << 30)) return PTG_ERR_INVALID;
     return PTG_OK;
 }

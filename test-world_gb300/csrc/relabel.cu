@@ -18,6 +18,7 @@
 // and medium rows reordered by neighbour group, rows of 4096+ edges by whole
 // CTAs in the caller's order).
 #include <algorithm>
+#include <cmath>
 #include <vector>
 
 #include "ptg_device.cuh"
@@ -273,6 +274,8 @@ __global__ void k_map_ids(uint32_t *ids, uint32_t k, const uint32_t *newid) {
 
 // out[r * n + v] = tmp[r * n + newid[v]] for rows r < k (caller order out;
 // gathering measured faster than scattering through perm)
+// (one thread maps a vertex in every row: measured faster than a row per
+// grid row)
 template <class T>
 __global__ void __launch_bounds__(kBlock) k_unpermute(const T *tmp, const uint32_t *newid, uint64_t n, uint32_t k,
                                                       T *out) {
@@ -305,7 +308,7 @@ inline void swap_buf(DevBuf &a, DevBuf &b) {
 }
 
 template <class OffT>
-void relabel_impl(ptg_graph *g) {
+bool relabel_impl(ptg_graph *g, bool always) {
     ptg_ctx *ctx = g->ctx;
     cudaStream_t st = ctx->stream;
     const uint64_t n = g->n, m = g->m;
@@ -335,6 +338,17 @@ void relabel_impl(ptg_graph *g) {
     }
     gstart[kVB] = acc;
     PTG_REQUIRE(acc == n, PTG_ERR_CUDA, "vertex grouping lost vertices");
+    if (!always) {
+        // grouping pays where degrees are skewed: at least a fifth of the
+        // edges (estimated per group) at vertices of 8x the mean degree
+        uint64_t active = n - (gstart[kVB] - gstart[kVB - 1]);
+        double mean = active ? (double)m / (double)active : 0.0, high = 0.0;
+        for (int k = 0; k < kVB - 1; k++) {
+            double lo = std::ldexp(1.0, 31 - k);
+            if (lo >= 8.0 * mean) high += 1.5 * lo * (double)(gstart[k + 1] - gstart[k]);
+        }
+        if (high < 0.2 * (double)m) return false;
+    }
     PTG_CUDA_TRY(cudaMemcpyAsync(cnt.p, h.data(), h.size() * 4, cudaMemcpyHostToDevice, st));
     launch(ctx, "k_vg_fill", k_vg_fill<OffT>, nb, 32, 0, st, off, n, per, nb, (const uint32_t *)cnt.p,
            perm.as<uint32_t>(), newid.as<uint32_t>());
@@ -389,20 +403,22 @@ void relabel_impl(ptg_graph *g) {
     swap_buf(g->d_newid, newid);
     g->relabeled = true;
     g->device_bytes += n * 8;
+    return true;
 }
 
 }  // namespace
 
 bool relabel_graph(ptg_graph *g) {
-    if (g->out_of_core || !g->symmetric || g->m == 0 || g->ctx->tuning.vertex_order == 0) return false;
+    const uint32_t vo = g->ctx->tuning.vertex_order;
+    if (g->out_of_core || !g->symmetric || g->m == 0 || vo == 0) return false;
+    // small graphs live in L2 anyway; the mapping launches would cost more
+    if (vo == 1 && g->m < (1ull << 20)) return false;
     // the rebuild holds both copies of the edge arrays for a moment
     size_t dfree = 0, dtot = 0;
     PTG_CUDA_TRY(cudaMemGetInfo(&dfree, &dtot));
     uint64_t need = (g->n + 1) * (g->off64 ? 8 : 4) + g->m * (g->weighted ? 8 : 4) + g->n * 8 + (256ull << 20);
     if (need > dfree) return false;
-    if (g->off64) relabel_impl<unsigned long long>(g);
-    else relabel_impl<uint32_t>(g);
-    return true;
+    return g->off64 ? relabel_impl<unsigned long long>(g, vo == 2) : relabel_impl<uint32_t>(g, vo == 2);
 }
 
 void map_sources_dev(ptg_graph *g, uint32_t *d_ids, uint32_t k) {

@@ -32,3 +32,13 @@ def ctx(ptg):
     c = ptg.Ctx(0)
     yield c
     c.close()
+
+
+@pytest.fixture(scope="session")
+def ctx_grouped(ptg):
+    """A context that stores every resident symmetric graph degree-grouped,
+    however small (the default tuning groups graphs of 2^20+ edges)."""
+    c = ptg.Ctx(0)
+    c.set_tuning(vertex_order=2)
+    yield c
+    c.close()

@@ -35,14 +35,15 @@ def configs(ptg, m):
 
 
 @pytest.mark.parametrize("path", GOLD, ids=IDS)
-@pytest.mark.parametrize("cfgname", ["resident", "ooc_prefix", "ooc_none_3buf"])
-def test_bfs_sssp_cc_match_reference(ptg, ctx, path, cfgname):
+@pytest.mark.parametrize("cfgname", ["resident", "resident_grouped", "ooc_prefix", "ooc_none_3buf"])
+def test_bfs_sssp_cc_match_reference(ptg, ctx, ctx_grouped, path, cfgname):
     g = load(path)
     sym = bool(g["symmetric"][0])
-    cfg = configs(ptg, g["col"].size)[cfgname]
-    G = ctx.graph(g["off"], g["col"], g["w"], symmetric=sym, config=cfg)
+    c = ctx_grouped if cfgname == "resident_grouped" else ctx
+    cfg = configs(ptg, g["col"].size).get(cfgname)
+    G = c.graph(g["off"], g["col"], g["w"], symmetric=sym, config=cfg)
     info = G.info()
-    if cfgname != "resident" and g["col"].size > 16:
+    if cfgname.startswith("ooc") and g["col"].size > 16:
         assert info["out_of_core"] == 1
     for i, s in enumerate(g["sources"]):
         s = int(s)

@@ -31,7 +31,9 @@ def _requests(gs, count, seed):
     return reqs
 
 
-def test_results_alone_equal_in_mix(ptg, ctx, oracle):
+@pytest.mark.parametrize("ctxname", ["ctx", "ctx_grouped"])
+def test_results_alone_equal_in_mix(ptg, oracle, request, ctxname):
+    ctx = request.getfixturevalue(ctxname)  # graphs as given / degree-grouped
     gs = _graphs(ptg)
     srv = ptg.Server(ctx, lanes=3)
     gids = [srv.upload(off, col, w)[0] for off, col, w in gs]

@@ -14,16 +14,16 @@ import pytest
 PR_RTOL = 1e-6  # max per-vertex relative error vs the FP64 oracle
 
 # every knob away from its default (and inside its range)
-OFF_DEFAULT = {"bfs_alpha": 6.0, "bfs_beta": 36.0, "sssp_delta_scale": 2.0, "expand_ctas_per_sm": 3,
+OFF_DEFAULT = {"bfs_alpha": 6.0, "bfs_beta": 36.0, "sssp_delta_scale": 0.5, "expand_ctas_per_sm": 3,
                "pr_ctas_per_sm": 5, "pr_mid": 16, "pr_chunk": 1024, "ms_pull_small": 8, "ms_pull_chunk": 256,
                "vertex_order": 0, "partition_bytes": 1 << 20}
 
 
 def test_builtin_values(ptg):
     d = ptg.tuning_defaults()
-    assert d == {"bfs_alpha": 15.0, "bfs_beta": 18.0, "sssp_delta_scale": 0.5, "expand_ctas_per_sm": 8,
-                 "pr_ctas_per_sm": 8, "pr_mid": 64, "pr_chunk": 4096, "ms_pull_small": 32,
-                 "ms_pull_chunk": 1024, "vertex_order": 1, "partition_bytes": 256 << 20}
+    assert d == {"bfs_alpha": 15.0, "bfs_beta": 18.0, "sssp_delta_scale": 2.0, "expand_ctas_per_sm": 4,
+                 "pr_ctas_per_sm": 8, "pr_mid": 256, "pr_chunk": 4096, "ms_pull_small": 32,
+                 "ms_pull_chunk": 1024, "vertex_order": 1, "partition_bytes": 32 << 20}
     assert ptg.tuning_valid(d)
     assert ptg.tuning_valid(OFF_DEFAULT)
 
@@ -33,7 +33,7 @@ def test_builtin_values(ptg):
     {"ms_pull_chunk": 100}, {"ms_pull_chunk": 16}, {"ms_pull_small": 0}, {"ms_pull_small": 5000},
     {"expand_ctas_per_sm": 0}, {"expand_ctas_per_sm": 33}, {"pr_ctas_per_sm": 0},
     {"bfs_alpha": 0.0}, {"bfs_alpha": math.nan}, {"bfs_beta": math.inf}, {"sssp_delta_scale": -1.0},
-    {"partition_bytes": 4096}, {"partition_bytes": 1 << 40}, {"vertex_order": 2},
+    {"partition_bytes": 4096}, {"partition_bytes": 1 << 40}, {"vertex_order": 3},
 ])
 def test_out_of_range_rejected(ptg, bad):
     assert not ptg.tuning_valid(bad)
@@ -158,7 +158,7 @@ def test_vertex_order_keeps_results(ptg, oracle, tctx, case):
     deg = np.diff(off.astype(np.int64))
     srcs = np.random.default_rng(9).choice(np.nonzero(deg)[0], 5, replace=False).astype(np.uint32)
     res = {}
-    for order in (0, 1):
+    for order in (0, 2):  # 2: grouped whatever the size
         tctx.set_tuning(vertex_order=order)
         G = tctx.graph(off, col, w, symmetric=True)
         r = {"bfs": [G.bfs(int(s)) for s in srcs], "sssp": [G.sssp(int(s)) for s in srcs], "cc": G.cc(),
@@ -168,7 +168,7 @@ def test_vertex_order_keeps_results(ptg, oracle, tctx, case):
         res[order] = r
         G.close()
     tctx.set_tuning()
-    a, b = res[0], res[1]
+    a, b = res[0], res[2]
     for i, s in enumerate(srcs):
         ref_b = oracle.bfs(off, col, int(s), method="queue")
         ref_s = oracle.sssp(off, col, w, int(s))
@@ -180,7 +180,7 @@ def test_vertex_order_keeps_results(ptg, oracle, tctx, case):
         nz = pref > 1e-30
         assert (np.abs(b["ppr"][i][nz] - pref[nz]) / pref[nz]).max() < PR_RTOL
     ref_cc = oracle.cc(off, col, method="unionfind")
-    for order in (0, 1):
+    for order in (0, 2):
         assert (res[order]["cc"] == ref_cc).all() and (res[order]["ccref"] == ref_cc).all()
     pr_ref = oracle.pagerank(off, col)
     assert (np.abs(b["pr"].astype(np.float64) - pr_ref) / pr_ref).max() < PR_RTOL
