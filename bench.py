@@ -35,8 +35,9 @@ PEAKS_FILE = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of the SpMV kernels of one
 # PageRank iteration (k_pr_small/mid/big/chunks/long) on RMAT scale 22:
-# 670.73 MB + 5.08 MB over n + m = 4,194,304 + 128,307,638 items
-PR_DRAM_BYTES_PER_ITEM = (670.733312e6 + 5.081856e6) / (4194304 + 128307638)
+# 584.27 MB + 1.42 MB over n + m = 4,194,304 + 128,307,638 items (built-in tuning:
+# degree-grouped vertex order)
+PR_DRAM_BYTES_PER_ITEM = (584.270848e6 + 1.417984e6) / (4194304 + 128307638)
 
 
 def make_ctx(args, device):
