@@ -82,13 +82,16 @@ struct Lane {
 };
 
 // Device bytes a lane's workspace needs for a batch of k (an estimate of the
-// buffers the multi-source passes grow).
-uint64_t batch_bytes(uint32_t kind, uint64_t n, uint64_t m, uint32_t k) {
+// buffers the multi-source passes grow).  On a degree-grouped graph the
+// results pass through buffers in the stored order first: the k level rows
+// of a multi-source BFS, one row of the single-source paths.
+uint64_t batch_bytes(uint32_t kind, uint64_t n, uint64_t m, uint32_t k, bool regrouped) {
     uint64_t q = 2 * n * 4 + 2 * (n + 1) * 8 + (m / kTile + 4) * 4;
     uint64_t rows = (uint64_t)k * n * 4;
+    if (regrouped) q += 2 * n * 4;
     if (kind == PTG_Q_BFS) {
         uint64_t W = k <= 64 ? 1 : (k <= 128 ? 2 : 4);
-        return 3 * n * 8 * W + rows + q;
+        return 3 * n * 8 * W + rows * (regrouped ? 2 : 1) + q;
     }
     if (kind == PTG_Q_SSSP) return n * 64 * 4 + 2 * n * 8 + rows + q;
     return 2 * n * 32 * 4 + rows + (m / 2048 + 1) * 32 * 8;  // PPR
@@ -96,7 +99,8 @@ uint64_t batch_bytes(uint32_t kind, uint64_t n, uint64_t m, uint32_t k) {
 
 uint64_t ws_bytes(const Workspace &w) {
     const DevBuf *b[] = {&w.value, &w.q[0], &w.q[1], &w.bm[0], &w.bm[1], &w.farbm, &w.vis, &w.scan, &w.rowstart,
-                         &w.tiles, &w.bsum, &w.ctl, &w.aux, &w.aux2, &w.flags, &w.ms[0], &w.ms[1], &w.ms[2]};
+                         &w.tiles, &w.bsum, &w.ctl, &w.aux, &w.aux2, &w.flags, &w.ms[0], &w.ms[1], &w.ms[2],
+                         &w.relab[0], &w.relab[1]};
     uint64_t s = 0;
     for (auto *x : b) s += x->bytes;
     return s;
@@ -259,7 +263,7 @@ bool take_batch(ptg_server *s, Batch &b) {
     uint64_t left = s->budget > s->graph_bytes ? s->budget - s->graph_bytes : 0;
     uint64_t share = left / s->lanes.size();
     const uint32_t kd = best->first.second;
-    while (k > 1 && batch_bytes(kd, n, m, k) > share) k = (k + 1) / 2;
+    while (k > 1 && batch_bytes(kd, n, m, k, e.g->relabeled) > share) k = (k + 1) / 2;
     // one fused pass for k requests, or a single-source query: whichever the
     // measured costs say is cheaper (a single query is measured first, then a
     // pass).  A lane takes one request at a time when it runs singles, so the
