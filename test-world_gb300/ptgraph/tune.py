@@ -172,10 +172,12 @@ def _same(kind, a, b):
 
 
 def tune(ctx, scale=22, seed=7, repeats=3, knobs=None, min_gain=0.02, n_bfs=16, n_sssp=4, n_ms=64,
-         ooc_scale=None, log=print):
+         ooc_scale=None, log=print, bench=None):
     """Sweep the knobs on `ctx`'s device; returns the JSON document (dict).
 
-    The context is left with the chosen tuning applied."""
+    The context is left with the chosen tuning applied.  `bench` replaces the
+    RMAT workloads (an object with fresh_graph(), run(kind) -> (ms, result),
+    close() and ooc_scale)."""
     knobs = list(knobs or CANDIDATES)
     for k in knobs:
         if k not in CANDIDATES:
@@ -183,7 +185,8 @@ def tune(ctx, scale=22, seed=7, repeats=3, knobs=None, min_gain=0.02, n_bfs=16, 
     ctx.set_tuning()  # start from the built-in values
     best = ctx.tuning()
     defaults = dict(best)
-    bench = _Bench(ctx, scale, seed, n_bfs, n_sssp, n_ms, ooc_scale if ooc_scale else scale)
+    if bench is None:
+        bench = _Bench(ctx, scale, seed, n_bfs, n_sssp, n_ms, ooc_scale if ooc_scale else scale)
     reference = {}     # workload -> result under the default tuning
     default_ms = {}
     sweeps = {}

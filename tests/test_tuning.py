@@ -206,3 +206,68 @@ def test_autotuner_small_run(ptg, tctx, tmp_path):
     tctx.set_tuning()
     assert tctx.load_tuning(str(path)) == doc["tuning"]
     tctx.set_tuning()
+
+
+class _FakeCtx:
+    """Context stand-in for the sweep logic (the library validates the knobs)."""
+
+    def __init__(self, ptg):
+        self.ptg = ptg
+        self.t = ptg.tuning_defaults()
+
+    def set_tuning(self, values=None, **kw):
+        v = dict(self.ptg.tuning_defaults())
+        v.update(values or {})
+        v.update(kw)
+        assert self.ptg.tuning_valid(v)
+        self.t = v
+
+    def tuning(self):
+        return dict(self.t)
+
+    def device_info(self):
+        return {"sm_count": 152, "hbm_bytes": 1 << 38}
+
+
+class _FakeBench:
+    """Times that depend on the knobs; one candidate gives a different result."""
+    ooc_scale = 0
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+
+    def fresh_graph(self):
+        pass
+
+    def close(self):
+        pass
+
+    def run(self, kind):
+        t = self.ctx.t
+        if kind == "pagerank":
+            ms = 10.0 + abs(t["pr_mid"] - 128) / 100.0  # fastest at 128
+            return ms, np.ones(4, dtype=np.float32)
+        if kind == "bfs":
+            ms = 10.0 - (0.5 if t["bfs_alpha"] == 6.0 else 0.0) - (0.05 if t["bfs_alpha"] == 22.0 else 0.0)
+            res = [np.arange(4, dtype=np.uint32) + (1 if t["bfs_alpha"] == 6.0 else 0)]
+            return ms, res
+        if kind == "sssp":
+            return 10.0 - 0.1 * t["sssp_delta_scale"], [np.zeros(4, dtype=np.uint32)]
+        raise ValueError(kind)
+
+
+def test_sweep_logic_without_gpu(ptg):
+    from ptgraph import tune
+    ctx = _FakeCtx(ptg)
+    doc = tune.tune(ctx, repeats=2, knobs=["pr_mid", "bfs_alpha", "sssp_delta_scale"], log=lambda *a: None,
+                    bench=_FakeBench(ctx))
+    # pr_mid: 128 is 1.28 ms (11%) faster than the built-in 256 -> chosen
+    assert doc["tuning"]["pr_mid"] == 128
+    # bfs_alpha: 6 is fastest but changes the result -> rejected; 22 is only 0.5% faster -> kept
+    assert doc["tuning"]["bfs_alpha"] == 15.0
+    rows = {r["value"]: r for r in doc["sweeps"]["bfs_alpha"]["candidates"]}
+    assert rows[6.0]["same_result"] is False and rows[22.0]["same_result"] is True
+    # sssp_delta_scale: larger is faster by more than 2% -> the largest candidate
+    assert doc["tuning"]["sssp_delta_scale"] == max(tune.CANDIDATES["sssp_delta_scale"])
+    assert ctx.tuning() == doc["tuning"]
+    json.dumps(doc)  # serialisable as written by the CLI
