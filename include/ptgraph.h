@@ -270,6 +270,9 @@ typedef struct ptg_graph_info {
     uint64_t partition_edges;     /* edges per partition                          */
     uint64_t resident_edges;      /* edges in HBM                                 */
     uint64_t device_bytes;        /* HBM held by the graph                        */
+    uint32_t degree_grouped;      /* 1: stored degree-grouped (ptg_tuning.vertex_order);
+                                     ids are mapped in and out                     */
+    uint32_t reserved;
 } ptg_graph_info;
 ptg_status ptg_graph_info_get(const ptg_graph *g, ptg_graph_info *info);
 

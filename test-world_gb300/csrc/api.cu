@@ -590,6 +590,8 @@ ptg_status ptg_graph_info_get(const ptg_graph *g, ptg_graph_info *info) {
     info->partition_edges = g->partition_edges;
     info->resident_edges = g->resident_edges;
     info->device_bytes = g->device_bytes;
+    info->degree_grouped = g->relabeled ? 1u : 0u;
+    info->reserved = 0;
     return PTG_OK;
 }
 

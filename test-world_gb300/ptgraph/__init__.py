@@ -90,7 +90,8 @@ class GraphInfo(ctypes.Structure):
                 ("weighted", ctypes.c_uint32), ("out_of_core", ctypes.c_uint32),
                 ("offsets_u64", ctypes.c_uint32), ("partitions", ctypes.c_uint64),
                 ("resident_partitions", ctypes.c_uint64), ("partition_edges", ctypes.c_uint64),
-                ("resident_edges", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64)]
+                ("resident_edges", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64),
+                ("degree_grouped", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class HostCsr(ctypes.Structure):

@@ -43,6 +43,7 @@ def test_bfs_sssp_cc_match_reference(ptg, ctx, ctx_grouped, path, cfgname):
     cfg = configs(ptg, g["col"].size).get(cfgname)
     G = c.graph(g["off"], g["col"], g["w"], symmetric=sym, config=cfg)
     info = G.info()
+    assert info["degree_grouped"] == (cfgname == "resident_grouped" and sym and g["col"].size > 0)
     if cfgname.startswith("ooc") and g["col"].size > 16:
         assert info["out_of_core"] == 1
     for i, s in enumerate(g["sources"]):

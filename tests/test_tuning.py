@@ -161,6 +161,7 @@ def test_vertex_order_keeps_results(ptg, oracle, tctx, case):
     for order in (0, 2):  # 2: grouped whatever the size
         tctx.set_tuning(vertex_order=order)
         G = tctx.graph(off, col, w, symmetric=True)
+        assert G.info()["degree_grouped"] == (1 if order == 2 else 0)
         r = {"bfs": [G.bfs(int(s)) for s in srcs], "sssp": [G.sssp(int(s)) for s in srcs], "cc": G.cc(),
              "ccref": G.cc(flags=ptg.PTG_REFERENCE_SCHEDULE), "pr": G.pagerank(),
              "ppr": [G.ppr(int(s)) for s in srcs], "pprb": G.ppr_batch(srcs), "msb": G.msbfs(srcs),
