@@ -144,3 +144,14 @@ def test_partition_planner_resident_none(ptg):
                                resident_policy=ptg.PTG_RESIDENT_NONE)
     P, R, _, _ = ptg.plan_partitions(off, 8, 0, cfg)
     assert R == 0 and P > 1
+
+
+def test_default_partition_size_is_the_tuned_one(ptg):
+    """A config without a partition size takes the context's tuned size; the
+    host-only planner (no context) uses the built-in tuning's 32 MiB."""
+    cfg = ptg.partition_config(force_out_of_core=1, device_budget_bytes=1 << 20)
+    assert cfg.partition_bytes == 0
+    assert ptg.tuning_defaults()["partition_bytes"] == 32 << 20
+    off = np.arange(0, (1 << 24) + 1, 4, dtype=np.uint64)  # 4M vertices of 4 edges, 16M edges
+    P, R, PE, _ = ptg.plan_partitions(off, 8, 0, cfg)
+    assert PE == (32 << 20) // 8 and P == (int(off[-1]) + PE - 1) // PE
