@@ -108,7 +108,19 @@ std::vector<uint64_t> host_offsets(const ptg_csr *c) {
     return o;
 }
 
-void plan(uint64_t n, uint64_t m, const uint64_t *off, uint64_t bpe, const ptg_partition_config *cfg_in,
+// The caller's offsets read in place: u32 or u64, n or n + 1 entries (the
+// reference's n-entry form ends at m).
+struct HostOffsets {
+    const void *p;
+    bool u64, sentinel;
+    uint64_t n, m;
+    uint64_t operator[](uint64_t i) const {
+        if (i == n && !sentinel) return m;
+        return u64 ? static_cast<const uint64_t *>(p)[i] : static_cast<const uint32_t *>(p)[i];
+    }
+};
+
+void plan(uint64_t n, uint64_t m, const HostOffsets &off, uint64_t bpe, const ptg_partition_config *cfg_in,
           uint64_t device_free, uint64_t &P, uint64_t &R, uint64_t &PE, std::vector<uint64_t> *first) {
     ptg_partition_config cfg;
     ptg_partition_config_default(&cfg);
@@ -135,8 +147,13 @@ void plan(uint64_t n, uint64_t m, const uint64_t *off, uint64_t bpe, const ptg_p
         for (uint64_t p = 0; p < P; p++) {
             uint64_t e = p * PE;
             // owner of edge e: last vertex with off[v] <= e
-            uint64_t v = (uint64_t)(std::upper_bound(off, off + n, e) - off);
-            (*first)[p] = v ? v - 1 : 0;
+            uint64_t lo = 0, hi = n;  // first v in [0, n) with off[v] > e
+            while (lo < hi) {
+                uint64_t mid = lo + (hi - lo) / 2;
+                if (off[mid] <= e) lo = mid + 1;
+                else hi = mid;
+            }
+            (*first)[p] = lo ? lo - 1 : 0;
         }
         (*first)[P] = n - 1;
     }
@@ -226,7 +243,7 @@ ptg_status ptg_plan_partitions(uint64_t n, uint64_t m, const uint64_t *offsets_n
     if (!offsets_n1 || n == 0 || bytes_per_edge == 0 || !num_partitions) return PTG_ERR_INVALID;
     uint64_t P, R, PE;
     std::vector<uint64_t> first;
-    plan(n, m, offsets_n1, bytes_per_edge, cfg, device_free_bytes, P, R, PE,
+    plan(n, m, HostOffsets{offsets_n1, true, true, n, m}, bytes_per_edge, cfg, device_free_bytes, P, R, PE,
          part_first_vertex ? &first : nullptr);
     *num_partitions = P;
     if (resident_partitions) *resident_partitions = R;
@@ -407,7 +424,10 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
         g->symmetric = (csr->flags & PTG_CSR_SYMMETRIC) != 0;
         g->weighted = csr->weight != nullptr || csr->edges_aos != nullptr;
         g->off64 = csr->m >= (1ull << 32);
-        std::vector<uint64_t> off = host_offsets(csr);
+        // the caller's offsets are read in place (no host copy): the device
+        // validation pass checks that they never decrease
+        const HostOffsets off{csr->offsets, csr->offset_type == PTG_OFFSETS_U64,
+                              csr->offset_form == PTG_FORM_SENTINEL, g->n, g->m};
         PTG_REQUIRE(off[0] == 0 && off[g->n] == g->m, PTG_ERR_INVALID,
                     "offsets must start at 0 and end at m");
         ptg_partition_config cfg;
@@ -425,7 +445,7 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
         uint64_t reserve = 48ull * g->n + (512ull << 20);
         uint64_t usable = dfree > reserve ? dfree - reserve : 0;
         uint64_t P, R, PE;
-        plan(g->n, g->m, off.data(), bpe, &cfg, usable, P, R, PE, &g->part_first_vertex);
+        plan(g->n, g->m, off, bpe, &cfg, usable, P, R, PE, &g->part_first_vertex);
         if ((cfg.resident_policy == PTG_RESIDENT_HOT || cfg.resident_policy == PTG_RESIDENT_HUBS) && R < P) {
             // the device budget holds partition slots instead of a prefix
             g->cache_slots = (uint32_t)R;
@@ -444,8 +464,21 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
         // offsets
         size_t osz = g->off64 ? 8 : 4;
         g->d_off.ensure((g->n + 1) * osz);
-        if (g->off64) {
-            PTG_CUDA_TRY(cudaMemcpyAsync(g->d_off.p, off.data(), (g->n + 1) * 8, cudaMemcpyHostToDevice, st));
+        if (off.u64 == g->off64) {
+            // same width: straight from the caller's array (n entries, then
+            // the sentinel m when the caller's form has none)
+            uint64_t last = g->m;
+            uint32_t last32 = (uint32_t)g->m;
+            uint64_t cnt = off.sentinel ? g->n + 1 : g->n;
+            PTG_CUDA_TRY(cudaMemcpyAsync(g->d_off.p, csr->offsets, cnt * osz, cudaMemcpyHostToDevice, st));
+            if (!off.sentinel)
+                PTG_CUDA_TRY(cudaMemcpyAsync(static_cast<char *>(g->d_off.p) + g->n * osz,
+                                             g->off64 ? (const void *)&last : (const void *)&last32, osz,
+                                             cudaMemcpyHostToDevice, st));
+            PTG_CUDA_TRY(cudaStreamSynchronize(st));
+        } else if (g->off64) {
+            std::vector<uint64_t> o = host_offsets(csr);
+            PTG_CUDA_TRY(cudaMemcpyAsync(g->d_off.p, o.data(), (g->n + 1) * 8, cudaMemcpyHostToDevice, st));
             PTG_CUDA_TRY(cudaStreamSynchronize(st));
         } else {
             std::vector<uint32_t> o32(g->n + 1);
@@ -565,7 +598,7 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
                 g->d_part_hits.ensure(P * 8);
                 g->h_part_hits.ensure(P * 8);
                 g->device_bytes += (uint64_t)g->cache_slots * PE * bpe;  // taken as partitions turn hot
-                if (g->cache_static) place_hubs(g, off, PE, st);
+                if (g->cache_static) place_hubs(g, host_offsets(csr), PE, st);
             }
         }
     });
