@@ -300,6 +300,7 @@ ptg_status ptg_ctx_set_tuning(ptg_ctx *ctx, const ptg_tuning *t) {
 
 ptg_status ptg_ctx_get_tuning(const ptg_ctx *ctx, ptg_tuning *t) {
     if (!ctx || !t) return PTG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(const_cast<ptg_ctx *>(ctx)->mu);  // a query in flight keeps its tuning
     *t = ctx->tuning;
     return PTG_OK;
 }
