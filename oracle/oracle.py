@@ -61,6 +61,7 @@ def lib():
             "orc_mt_sssp": [u64, _u64p, _u32p, _u32p, u32, u32, _u32p],
             "orc_mt_cc": [u64, _u64p, _u32p, u32, _u32p],
             "orc_mt_pagerank": [u64, _u64p, _u32p, f64, u32, u32, _f32p],
+            "orc_sssp_certificate": [u64, _u64p, _u32p, _u32p, u32, u32, u32, _u32p, _u64p],
         }
         for name, argt in sigs.items():
             fn = getattr(L, name)
@@ -112,6 +113,19 @@ def sssp(off, col, w, src, base=1, unreached=UNREACHED, method="dijkstra"):
     if rc != 0:
         raise OverflowError("SSSP distance does not fit in u32")
     return out
+
+
+def sssp_certificate(off, col, w, src, dist, base=1, unreached=UNREACHED):
+    """(ok, failed condition, vertex): checks dist as the exact SSSP answer
+    from src in one pass over the edges (ptg_oracle.h, orc_sssp_certificate)."""
+    n, off, col, w = _prep(off, col, w)
+    dist = np.ascontiguousarray(dist, dtype=np.uint32)
+    if dist.size != n:
+        raise ValueError("dist must have n entries")
+    bad = np.zeros(1, dtype=np.uint64)
+    rc = lib().orc_sssp_certificate(n, _p(off, _u64p), _p(col, _u32p), _p(w, _u32p), src, base, unreached,
+                                    _p(dist, _u32p), _p(bad, _u64p))
+    return rc == 0, rc, int(bad[0])
 
 
 def cc(off, col, method="frontier"):

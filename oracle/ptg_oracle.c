@@ -238,3 +238,41 @@ void orc_ppr_f64(uint64_t n, const uint64_t *off, const uint32_t *col, uint32_t 
                  uint32_t iters, double *rank) {
     pr_core(n, off, col, d, iters, 1, src, rank);
 }
+
+/* ------------------------------------------------------------------------ */
+/* SSSP certificate (see ptg_oracle.h): one pass over the edges marks tight */
+/* in-edges and checks the triangle inequality.                             */
+/* ------------------------------------------------------------------------ */
+int orc_sssp_certificate(uint64_t n, const uint64_t *off, const uint32_t *col, const uint32_t *w,
+                         uint32_t src, uint32_t base, uint32_t unreached_val, const uint32_t *dist,
+                         uint64_t *bad) {
+    if (bad) *bad = 0;
+    if (src >= n || dist[src] != base) {
+        if (bad) *bad = src;
+        return 1;
+    }
+    unsigned char *tight = (unsigned char *)calloc(n ? n : 1, 1);
+    int rc = 0;
+    for (uint64_t u = 0; u < n && !rc; u++) {
+        if (dist[u] == unreached_val) continue;
+        for (uint64_t e = off[u]; e < off[u + 1]; e++) {
+            uint32_t v = col[e];
+            uint64_t cand = (uint64_t)dist[u] + (uint64_t)w[e];
+            uint64_t dv = dist[v] == unreached_val ? ~0ull : (uint64_t)dist[v];
+            if (dv > cand) {
+                rc = 2;
+                if (bad) *bad = v;
+                break;
+            }
+            if (dv == cand) tight[v] = 1;
+        }
+    }
+    for (uint64_t v = 0; v < n && !rc; v++) {
+        if (v != src && dist[v] != unreached_val && !tight[v]) {
+            rc = 3;
+            if (bad) *bad = v;
+        }
+    }
+    free(tight);
+    return rc;
+}

@@ -69,6 +69,19 @@ void orc_mt_cc(uint64_t n, const uint64_t *off, const uint32_t *col, uint32_t th
 void orc_mt_pagerank(uint64_t n, const uint64_t *off, const uint32_t *col, double d,
                      uint32_t iters, uint32_t threads, float *rank);
 
+/* Shortest-path certificate for graphs too large for Dijkstra here (the
+ * out-of-core scale; the check streams the CSR once, O(n + m)): dist is the
+ * exact SSSP answer from src (dist[src] = base, unreached = unreached_val)
+ * iff dist[src] == base, no edge u->v from a reached u has
+ * dist[v] > dist[u] + w (unreached v counts as infinite), and every reached
+ * v != src has an in-edge with dist[v] == dist[u] + w (a tight edge; with
+ * positive weights these form a shortest-path tree).  Returns 0 if the
+ * certificate holds, else 1 + the first failed condition's index and, in
+ * *bad, the vertex it failed at. */
+int orc_sssp_certificate(uint64_t n, const uint64_t *off, const uint32_t *col, const uint32_t *w,
+                         uint32_t src, uint32_t base, uint32_t unreached_val, const uint32_t *dist,
+                         uint64_t *bad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -170,6 +170,27 @@ def test_directed_rmat_out_of_core_vs_oracle(ptg, ctx, oracle):
     assert (G.cc() == oracle.cc(off, col)).all()
 
 
+def test_streamed_sssp_certificate_rmat20(ptg, ctx, oracle):
+    """The check used where Dijkstra on the host is out of reach (the
+    out-of-core scale): a one-pass shortest-path certificate over the CSR,
+    here on a directed RMAT-20 with three quarters of its edges streamed in
+    4 MiB partitions, from several sources."""
+    off, col, w = ptg.gen_rmat(20, 16, seed=3, symmetric=False, wmin=1, wmax=63)
+    edge_bytes = col.size * 8
+    cfg = ptg.partition_config(partition_bytes=4 << 20, device_budget_bytes=edge_bytes // 4, force_out_of_core=1)
+    G = ctx.graph(off, col, w, symmetric=False, config=cfg)
+    assert G.info()["out_of_core"] == 1
+    deg = np.diff(off.astype(np.int64))
+    for s in [0] + [int(x) for x in np.random.default_rng(8).choice(np.nonzero(deg)[0], 2, replace=False)]:
+        st = {}
+        d = G.sssp(s, stats=st)
+        ok, rc, v = oracle.sssp_certificate(off, col, w, s, d)
+        assert ok, (s, rc, v)
+        if s == 0:  # the top hub reaches most of the graph
+            assert st["partitions_streamed"] > 0
+    G.close()
+
+
 def test_bad_arguments(ptg, ctx):
     g = load(os.path.join(os.path.dirname(__file__), "golden", "path10.npz"))
     G = ctx.graph(g["off"], g["col"], symmetric=True)

@@ -79,3 +79,37 @@ def test_mt_pagerank_close_to_f64(oracle):
     r32 = oracle.mt_pagerank(g["off"], g["col"], 4)
     rel = np.abs(r32.astype(np.float64) - r64) / r64
     assert rel.max() < 1e-6
+
+
+@pytest.mark.parametrize("path", GOLD, ids=[os.path.basename(p)[:-4] for p in GOLD])
+def test_sssp_certificate_accepts_reference_distances(oracle, path):
+    g = load(path)
+    if "sssp" not in g or (g["w"] == 0).any():
+        pytest.skip("no weighted SSSP fixture with positive weights")
+    for i, s in enumerate(g["sources"]):
+        ok, rc, v = oracle.sssp_certificate(g["off"], g["col"], g["w"], int(s), g["sssp"][i])
+        assert ok, (rc, v)
+
+
+def test_sssp_certificate_rejects_planted_errors(oracle, ptg):
+    """Mistakes planted in a correct distance array (on the CPU) are caught."""
+    off, col, w = ptg.gen_rmat(12, 16, seed=7, symmetric=False, wmin=1, wmax=63)
+    d = oracle.sssp(off, col, w, 0)
+    assert oracle.sssp_certificate(off, col, w, 0, d)[0]
+    reached = np.nonzero((d != UMAX) & (np.arange(d.size) != 0))[0]
+    assert reached.size > 100
+    v = int(reached[reached.size // 2])
+    # too small: no tight in-edge left (or an out-edge it was tight for breaks)
+    bad = d.copy()
+    bad[v] = np.uint32(int(bad[v]) - 1)
+    assert oracle.sssp_certificate(off, col, w, 0, bad)[1] in (2, 3)
+    # too large: the in-edge that was tight now beats it
+    bad = d.copy()
+    bad[v] = np.uint32(int(bad[v]) + 1)
+    assert oracle.sssp_certificate(off, col, w, 0, bad)[1] == 2
+    bad = d.copy()
+    bad[v] = UMAX  # a reached vertex reported unreached
+    assert oracle.sssp_certificate(off, col, w, 0, bad)[1] == 2
+    bad = d.copy()
+    bad[0] = 2  # wrong source value
+    assert oracle.sssp_certificate(off, col, w, 0, bad)[1] == 1
