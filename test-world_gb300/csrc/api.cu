@@ -529,7 +529,16 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
         PTG_CUDA_TRY(cudaStreamSynchronize(st));
         PTG_REQUIRE(!(hbad & 1), PTG_ERR_INVALID, "offsets are not non-decreasing within [0, m]");
         PTG_REQUIRE(!(hbad & 2), PTG_ERR_INVALID, "an edge target is >= n");
-        relabel_graph(g);  // degree-grouped vertex order, when the tuning asks for it
+        // degree-grouped vertex order, when the tuning asks for it.  The
+        // rebuild holds two copies of the edges for a moment; if that memory
+        // is not there the graph stays in the caller's order (nothing was
+        // swapped yet: the rebuild's buffers are released on the way out).
+        try {
+            relabel_graph(g);
+        } catch (const Error &e) {
+            if (e.status != PTG_ERR_OOM) throw;
+            cudaGetLastError();
+        }
 
         if (g->out_of_core) {
             // host side of the streamed partitions: pinned SoA arrays
