@@ -60,6 +60,8 @@ def parse():
     p.add_argument("--sssp-sources", type=int, default=4)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-parity", action="store_true",
+                   help="skip the check of the suite's results against the oracle (run outside the timed region)")
     p.add_argument("--tuning", default="",
                    help="autotuner JSON (python -m ptgraph.tune) applied to every context; "
                         "default: the library's built-in tuning")
@@ -494,10 +496,15 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def make_workload(args):
-    import ptgraph
+def make_workload(args, gen=None):
+    """The suite's graph and sources.  gen: the RMAT generator to build it with
+    (the engine's ptgraph.gen_rmat by default; the CPU arm passes the oracle's
+    restatement, which gives the same graph, so it never maps the engine)."""
+    if gen is None:
+        import ptgraph
+        gen = ptgraph.gen_rmat
     t0 = time.time()
-    off, col, w = ptgraph.gen_rmat(args.scale, 16, 0.57, 0.19, 0.19, seed=2, symmetric=True, wmin=1, wmax=63)
+    off, col, w = gen(args.scale, 16, 0.57, 0.19, 0.19, seed=2, symmetric=True, wmin=1, wmax=63)
     gen_s = time.time() - t0
     n, m = off.size - 1, col.size
     deg = np.diff(off.astype(np.int64))
@@ -512,34 +519,82 @@ def teps_edges(levels, deg):
     return int(deg[reached].sum()) // 2
 
 
+# Weights of one suite step, per algorithm run: 64 BFS, 4 SSSP, CC, and 20
+# PageRank iterations (10 two-iteration runs).
+def suite_weights(args):
+    return {"bfs": args.sources, "sssp": args.sssp_sources, "cc": 1, "pr2": 10}
+
+
+def cpu_suite_sample(O, off, col, w, deg, sources, sssp_sources, threads, steps):
+    """The reference's algorithm on host cores (the oracle's multithreaded
+    restatement of its frontier label propagation, plus pull PageRank): each
+    step runs 1 BFS and 1 SSSP (sources cycling), CC and 2 PageRank
+    iterations, timed each.  Returns per-run mean times (s), their edges in
+    the suite's TEPS convention, and the sampled wall time per step."""
+    m = col.size
+    t = {"bfs": [], "sssp": [], "cc": [], "pr2": []}
+    e = {"bfs": [], "sssp": []}
+    walls = []
+    for step in range(steps):
+        w0 = time.perf_counter()
+        s = int(sources[step % sources.size])
+        t0 = time.perf_counter()
+        lv = O.mt_bfs(off, col, s, threads)
+        t["bfs"].append(time.perf_counter() - t0)
+        e["bfs"].append(teps_edges(lv, deg))
+        s = int(sssp_sources[step % sssp_sources.size])
+        t0 = time.perf_counter()
+        d = O.mt_sssp(off, col, w, s, threads)
+        t["sssp"].append(time.perf_counter() - t0)
+        e["sssp"].append(teps_edges(d, deg))
+        t0 = time.perf_counter()
+        O.mt_cc(off, col, threads)
+        t["cc"].append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        O.mt_pagerank(off, col, threads, iters=2)
+        t["pr2"].append(time.perf_counter() - t0)
+        walls.append(time.perf_counter() - w0)
+    mean = {k: sum(v) / len(v) for k, v in t.items()}
+    edges = {"bfs": sum(e["bfs"]) / len(e["bfs"]), "sssp": sum(e["sssp"]) / len(e["sssp"]),
+             "cc": m // 2, "pr2": 2 * (m // 2)}
+    return mean, edges, sum(walls) / len(walls)
+
+
+def composed_suite(mean, edges, weights):
+    """Suite GTEPS from per-run rates and the suite's weights: the sample's
+    per-algorithm times scaled to one suite step (64 BFS, 4 SSSP, CC, 20
+    PageRank iterations), so the CPU figure weighs the algorithms as the GPU
+    step does."""
+    ms = 1e3 * sum(weights[k] * mean[k] for k in weights)
+    e = sum(weights[k] * edges[k] for k in weights)
+    return e / (ms * 1e-3) / 1e9, ms, {k: edges[k] / mean[k] / 1e9 for k in weights}
+
+
 def run_reference(args, rank, pg):
-    """The reference's algorithm on host cores (the oracle's multithreaded restatement)."""
+    """The reference's algorithm on host cores (the oracle's multithreaded
+    restatement), on the suite's own graph built by the oracle's generator:
+    the engine's library is never loaded on this arm."""
     if rank != 0:
         return
     from oracle import oracle as O
     O.build()
-    off, col, w, deg, sources, _ = make_workload(args)
     threads = os.cpu_count() or 1
-    m = col.size
-    times, edges = [], []
-    for step in range(args.warmup + args.steps):
-        s = int(sources[step % sources.size])
-        t0 = time.perf_counter()
-        lv = O.mt_bfs(off, col, s, threads)
-        d = O.mt_sssp(off, col, w, s, threads)
-        O.mt_cc(off, col, threads)
-        O.mt_pagerank(off, col, threads, iters=2)
-        dt = time.perf_counter() - t0
-        e = 2 * teps_edges(lv, deg) + m // 2 + 2 * (m // 2)
-        if step >= args.warmup:
-            times.append(dt)
-            edges.append(e)
-    val = sum(edges) / sum(times) / 1e9
-    sample = "per step: 1 BFS + 1 SSSP (sources cycling over the 64) + CC + 2 PageRank iterations"
+    off, col, w, deg, sources, gen_s = make_workload(
+        args, gen=lambda *a, **k: O.gen_rmat(*a, threads=threads, **k))
+    if args.warmup:  # untimed warm-up steps
+        cpu_suite_sample(O, off, col, w, deg, sources, sources[:args.sssp_sources], threads, args.warmup)
+    mean, edges, wall = cpu_suite_sample(O, off, col, w, deg, sources, sources[:args.sssp_sources], threads,
+                                         args.steps)
+    val, suite_ms, rates = composed_suite(mean, edges, suite_weights(args))
+    sample = ("per step: 1 BFS + 1 SSSP (sources cycling over the suite's) + CC + 2 PageRank iterations, "
+              "each timed; value = the suite's edges / (64 x BFS + 4 x SSSP + CC + 10 x PageRank-2 mean times)")
     line = {"impl": "reference", "metric": "suite_gteps", "value": val, "unit": "GTEPS", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * sum(times) / len(times),
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * wall,
+            "suite_ms_composed": suite_ms, "per_algorithm_gteps": rates,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
-            "data": "synthetic", "config": workload_config(args),
+            "data": "synthetic (RMAT from the oracle's generator, seeded; the GPU arm's graph)",
+            "config": workload_config(args), "graph": {"n": int(off.size - 1), "m": int(col.size),
+                                                       "gen_s": round(gen_s, 2)},
             "cpu_baseline": {"value": val, "unit": "GTEPS", "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": val, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -632,25 +687,24 @@ def main():
     step_device()
     prof = ctx.profile_entries()
     ctx.profile(False)
-    per_alg = {}
-    st = {}
-    G.bfs(int(sources[0]), flags=ptgraph.PTG_OUT_DEVICE, stats=st, out=dev["bfs"])
-    per_alg["bfs_ms_src0"] = st["device_ms"]
     roof = roofline(prof, n, m, step_edges, G_bfs_edges, args)
+    algs = algorithm_rooflines(G, ptgraph, dev, sources, deg, n, m, args)
+    parity = None if args.no_parity else parity_check(G, off, col, w, sources, deg, dev, args)
 
     e2e = None
     if not args.no_e2e:
         e2e = e2e_measure(ctx, off32, col, w, sources, args, deg, step_edges, n, m)
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(off, col, w, sources, deg, m)
+        cpu = cpu_baseline(off, col, w, sources, deg, args)
     if rank == 0:
         line = {"metric": "suite_gteps", "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "wall_ms_per_step": 1e3 * wall / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
                 "data": "synthetic (RMAT generated on the host, seeded)", "config": workload_config(args),
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches // args.steps,
-                "clocks": clock_info, "kernel_profile_ms": {k: [c, round(t, 4)] for k, (c, t) in prof.items()},
+                "clocks": clock_info, "parity": parity, "algorithms": algs,
+                "kernel_profile_ms": {k: [c, round(t, 4)] for k, (c, t) in prof.items()},
                 "graph": {"n": n, "m": m, "gen_s": round(gen_s, 2)}}
         print(json.dumps(line))
 
@@ -694,6 +748,100 @@ def roofline(prof, n, m, step_edges, bfs_edges, args):
             "share_of_step": tot / sum(v[1] for v in prof.values())}
 
 
+def algorithm_rooflines(G, ptgraph, dev, sources, deg, n, m, args):
+    """Per algorithm, one run of each after the timed region: device time,
+    the algorithmic bytes of the byte models below, and their rate against
+    the measured HBM copy peak.  m_r = directed edges out of reached vertices.
+      BFS  4(n+1) + 4 m_r + 4n        (offsets, reached adjacency, levels)
+      SSSP 4(n+1) + 8 m_r + 4n        (settle-once: each reached edge's target
+                                       and weight once); edges_relaxed / m_r
+                                       is the redundancy over settle-once
+      CC   4(n+1) + 4m + 8n
+      PR   20 x (4(n+1) + 8m + 8n)"""
+    hbm, kind = peaks()
+    out = {}
+    rows = []
+    for s in sources[:args.sssp_sources]:
+        st = {}
+        G.bfs(int(s), flags=ptgraph.PTG_OUT_DEVICE, stats=st, out=dev["bfs"])
+        mr = 2 * teps_edges(dev["bfs"].cpu().numpy().view(np.uint32), deg)
+        rows.append(("bfs", st, mr))
+        st = {}
+        G.sssp(int(s), flags=ptgraph.PTG_OUT_DEVICE, stats=st, out=dev["sssp"])
+        rows.append(("sssp", st, 2 * teps_edges(dev["sssp"].cpu().numpy().view(np.uint32), deg)))
+    for name in ("bfs", "sssp"):
+        sel = [(st, mr) for k, st, mr in rows if k == name]
+        ms = sum(st["device_ms"] for st, _ in sel) / len(sel)
+        mr = sum(mr for _, mr in sel) / len(sel)
+        per = 4 * (n + 1) + (4 if name == "bfs" else 8) * mr + 4 * n
+        d = {"ms": ms, "bytes": per, "gbs": per / (ms * 1e-3) / 1e9, "m_r": mr,
+             "rounds": sum(st["iterations"] for st, _ in sel) / len(sel)}
+        d["frac"] = d["gbs"] / hbm
+        if name == "sssp":
+            d["edges_relaxed"] = sum(st["edges_relaxed"] for st, _ in sel) / len(sel)
+            d["redundancy_vs_settle_once"] = d["edges_relaxed"] / mr
+        else:
+            d["bottom_up_rounds"] = sum(st["bottom_up_rounds"] for st, _ in sel) / len(sel)
+        out[name] = d
+    st = {}
+    G.cc(flags=ptgraph.PTG_OUT_DEVICE, stats=st, out=dev["cc"])
+    per = 4 * (n + 1) + 4 * m + 8 * n
+    out["cc"] = {"ms": st["device_ms"], "bytes": per, "gbs": per / (st["device_ms"] * 1e-3) / 1e9}
+    out["cc"]["frac"] = out["cc"]["gbs"] / hbm
+    st = {}
+    G.pagerank(flags=ptgraph.PTG_OUT_DEVICE, stats=st, out=dev["pr"])
+    per = 20 * (4 * (n + 1) + 8 * m + 8 * n)
+    out["pagerank"] = {"ms": st["device_ms"], "bytes": per, "gbs": per / (st["device_ms"] * 1e-3) / 1e9}
+    out["pagerank"]["frac"] = out["pagerank"]["gbs"] / hbm
+    out["peak_gbs"] = hbm
+    out["peak_kind"] = kind
+    out["sources"] = "the %d SSSP sources (BFS from the same)" % args.sssp_sources
+    return out
+
+
+def parity_check(G, off, col, w, sources, deg, dev, args):
+    """The suite's results at the benchmarked size against the oracle (outside
+    the timed region): BFS from 4 of the sources against queue BFS, SSSP from
+    the SSSP sources by the one-pass shortest-path certificate (Dijkstra on the
+    host is too slow here), CC against union-find, PageRank (20 iterations,
+    FP32 on the GPU) against the FP64 oracle: max per-vertex relative error
+    (tolerance 1e-6) and the L1 error sum |r - r64| (and relative to sum r64)."""
+    import ptgraph
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    t0 = time.time()
+    res = {"checked": True, "scale": args.scale, "bfs_sources": 0, "bfs_equal": 0, "sssp_sources": 0,
+           "sssp_certified": 0}
+    for s in sources[:4]:
+        G.bfs(int(s), flags=ptgraph.PTG_OUT_DEVICE, out=dev["bfs"])
+        got = dev["bfs"].cpu().numpy().view(np.uint32)
+        res["bfs_sources"] += 1
+        res["bfs_equal"] += int(np.array_equal(got, O.bfs(off, col, int(s), method="queue")))
+    for s in sources[:args.sssp_sources]:
+        G.sssp(int(s), flags=ptgraph.PTG_OUT_DEVICE, out=dev["sssp"])
+        got = dev["sssp"].cpu().numpy().view(np.uint32)
+        ok, rc, bad = O.mt_sssp_certificate(off, col, w, int(s), got, threads)
+        res["sssp_sources"] += 1
+        res["sssp_certified"] += int(ok)
+        if not ok:
+            res.setdefault("sssp_failures", []).append({"src": int(s), "code": rc, "vertex": bad})
+    G.cc(flags=ptgraph.PTG_OUT_DEVICE, out=dev["cc"])
+    res["cc_equal"] = bool(np.array_equal(dev["cc"].cpu().numpy().view(np.uint32),
+                                          O.cc(off, col, method="unionfind")))
+    G.pagerank(flags=ptgraph.PTG_OUT_DEVICE, out=dev["pr"])
+    r = dev["pr"].cpu().numpy().astype(np.float64)
+    ref = O.mt_pagerank_f64(off, col, threads)
+    res["pr_max_rel"] = float((np.abs(r - ref) / ref).max())
+    res["pr_l1"] = float(np.abs(r - ref).sum())
+    res["pr_l1_rel"] = res["pr_l1"] / float(ref.sum())
+    res["pr_tolerance"] = 1e-6
+    res["ok"] = (res["bfs_equal"] == res["bfs_sources"] and res["sssp_certified"] == res["sssp_sources"] and
+                 res["cc_equal"] and res["pr_max_rel"] < 1e-6)
+    res["check_s"] = round(time.time() - t0, 1)
+    return res
+
+
 def e2e_measure(ctx, off32, col, w, sources, args, deg, step_edges, n, m):
     import torch
     import ptgraph
@@ -734,29 +882,19 @@ def e2e_measure(ctx, off32, col, w, sources, args, deg, step_edges, n, m):
             "path": "ptg_graph_create from pinned host CSR + ptg_bfs/sssp/cc/pagerank into host buffers"}
 
 
-def cpu_baseline(off, col, w, sources, deg, m):
+def cpu_baseline(off, col, w, sources, deg, args):
+    """The CPU port on all host cores over a bounded sample (2 steps of the
+    reference arm's sample), composed into the suite's weights."""
     from oracle import oracle as O
     O.build()
     threads = os.cpu_count() or 1
-    s = int(sources[0])
-    t0 = time.perf_counter()
-    lv = O.mt_bfs(off, col, s, threads)
-    t_bfs = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    O.mt_sssp(off, col, w, s, threads)
-    t_sssp = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    O.mt_cc(off, col, threads)
-    t_cc = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    O.mt_pagerank(off, col, threads, iters=2)
-    t_pr = time.perf_counter() - t0
-    e = teps_edges(lv, deg)
-    edges = 2 * e + m // 2 + 2 * (m // 2)
-    tot = t_bfs + t_sssp + t_cc + t_pr
-    return {"value": edges / tot / 1e9, "unit": "GTEPS", "cores": threads, "kind": "port",
-            "sample": "1 BFS + 1 SSSP (source 0 of 64) + CC + 2 PageRank iterations on the same graph",
-            "seconds": {"bfs": t_bfs, "sssp": t_sssp, "cc": t_cc, "pr2": t_pr}}
+    mean, edges, _ = cpu_suite_sample(O, off, col, w, deg, sources, sources[:args.sssp_sources], threads, 2)
+    val, suite_ms, rates = composed_suite(mean, edges, suite_weights(args))
+    return {"value": val, "unit": "GTEPS", "cores": threads, "kind": "port",
+            "sample": "2 x (1 BFS + 1 SSSP + CC + 2 PageRank iterations) on the same graph, composed into "
+                      "64 BFS + 4 SSSP + CC + 20 PageRank iterations",
+            "suite_ms_composed": suite_ms, "per_algorithm_gteps": rates,
+            "seconds": {k: round(v, 3) for k, v in mean.items()}}
 
 
 if __name__ == "__main__":

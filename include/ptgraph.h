@@ -85,7 +85,11 @@ enum {
 enum {
     PTG_CSR_SYMMETRIC = 1u << 0, /* every edge u->v has v->u: enables pull/bottom-up
                                     BFS, hooking CC and pull PageRank on the same CSR */
-    PTG_CSR_HOST_PINNED = 1u << 1 /* arrays already pinned (no registration needed) */
+    PTG_CSR_HOST_PINNED = 1u << 1, /* arrays already pinned (no registration needed) */
+    PTG_CSR_WIDE_OFFSETS = 1u << 2 /* keep 64-bit offsets on the device even when
+                                      m < 2^32 (they are 64-bit anyway from 2^32
+                                      edges on, which the reference's u32 offsets
+                                      cannot hold, ptGraph/main.cu:99-102)         */
 };
 
 typedef struct ptg_csr {
@@ -319,10 +323,14 @@ ptg_status ptg_ppr_batch(ptg_graph *g, const uint32_t *sources, uint32_t k, floa
  * inside the library, which every GPU that loads the library keeps until the
  * process exits; graphs above PTG_NOALLOC_MAX_VERTICES vertices are rejected
  * with PTG_ERR_UNSUPPORTED (bad pointers or src >= n: PTG_ERR_INVALID).  The
- * first call on a device looks up the scratch's device address (make that
- * first call before any stream capture).  All calls share the scratch, so
- * calls that overlap on the GPU race: serialize them.  The call returns when
- * the BFS has finished on `stream`. */
+ * CSR is checked on the device before any edge is read through it: offsets
+ * that do not start at 0, decrease, or do not end at m, and targets >= n,
+ * give PTG_ERR_INVALID (d_levels then holds no result).  The first call on a
+ * device looks up the scratch's device address (make that first call before
+ * any stream capture).  All calls share the scratch, so calls that overlap on
+ * the GPU race: serialize them.  The call synchronizes `stream` once per BFS
+ * level (it reads the next frontier's size back) and returns when the BFS has
+ * finished on it. */
 #define PTG_NOALLOC_MAX_VERTICES (1u << 20)
 #define PTG_NOALLOC_SCRATCH_BYTES ((16u << 20) + (64u << 10))
 ptg_status ptg_bfs_noalloc(const uint32_t *d_offsets, const uint32_t *d_col, uint32_t n,

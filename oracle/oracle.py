@@ -62,11 +62,17 @@ def lib():
             "orc_mt_cc": [u64, _u64p, _u32p, u32, _u32p],
             "orc_mt_pagerank": [u64, _u64p, _u32p, f64, u32, u32, _f32p],
             "orc_sssp_certificate": [u64, _u64p, _u32p, _u32p, u32, u32, u32, _u32p, _u64p],
+            "orc_mt_sssp_certificate": [u64, _u64p, _u32p, _u32p, u32, u32, u32, _u32p, u32, _u64p],
+            "orc_mt_pagerank_f64": [u64, _u64p, _u32p, f64, u32, u32, _f64p],
+            "orc_gen_rmat": [u32, u32, f64, f64, f64, u64, ctypes.c_int, u32, u32, u32,
+                             _u64p, _u64p, ctypes.POINTER(_u64p), ctypes.POINTER(_u32p),
+                             ctypes.POINTER(_u32p)],
+            "orc_free": [ctypes.c_void_p],
         }
         for name, argt in sigs.items():
             fn = getattr(L, name)
             fn.argtypes = argt
-            fn.restype = ctypes.c_int if name.startswith("orc_sssp") else None
+            fn.restype = ctypes.c_int if name.startswith(("orc_sssp", "orc_mt_sssp", "orc_gen")) else None
         _lib = L
     return _lib
 
@@ -128,6 +134,18 @@ def sssp_certificate(off, col, w, src, dist, base=1, unreached=UNREACHED):
     return rc == 0, rc, int(bad[0])
 
 
+def mt_sssp_certificate(off, col, w, src, dist, threads, base=1, unreached=UNREACHED):
+    """sssp_certificate on `threads` host cores (same return values)."""
+    n, off, col, w = _prep(off, col, w)
+    dist = np.ascontiguousarray(dist, dtype=np.uint32)
+    if dist.size != n:
+        raise ValueError("dist must have n entries")
+    bad = np.zeros(1, dtype=np.uint64)
+    rc = lib().orc_mt_sssp_certificate(n, _p(off, _u64p), _p(col, _u32p), _p(w, _u32p), src, base, unreached,
+                                       _p(dist, _u32p), threads, _p(bad, _u64p))
+    return rc == 0, rc, int(bad[0])
+
+
 def cc(off, col, method="frontier"):
     n, off, col, _ = _prep(off, col)
     out = np.empty(n, dtype=np.uint32)
@@ -148,6 +166,37 @@ def ppr(off, col, src, d=0.85, iters=20):
     out = np.empty(n, dtype=np.float64)
     lib().orc_ppr_f64(n, _p(off, _u64p), _p(col, _u32p), src, d, iters, _p(out, _f64p))
     return out
+
+
+def mt_pagerank_f64(off, col, threads, d=0.85, iters=20):
+    """FP64 PageRank of a symmetric CSR on `threads` host cores (pull form of pagerank())."""
+    n, off, col, _ = _prep(off, col)
+    out = np.empty(n, dtype=np.float64)
+    lib().orc_mt_pagerank_f64(n, _p(off, _u64p), _p(col, _u32p), d, iters, threads, _p(out, _f64p))
+    return out
+
+
+def gen_rmat(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1, symmetric=True, wmin=0, wmax=0,
+             threads=0):
+    """The benchmark's RMAT input, generated by the oracle's own restatement of
+    the generator: (offsets u64 n+1, col u32, weight u32 or None)."""
+    n = ctypes.c_uint64()
+    m = ctypes.c_uint64()
+    po, pc, pw = _u64p(), _u32p(), _u32p()
+    rc = lib().orc_gen_rmat(scale, edge_factor, a, b, c, seed, 1 if symmetric else 0, wmin, wmax,
+                            threads or (os.cpu_count() or 1), ctypes.byref(n), ctypes.byref(m),
+                            ctypes.byref(po), ctypes.byref(pc), ctypes.byref(pw))
+    if rc != 0:
+        raise MemoryError("orc_gen_rmat failed (%d)" % rc) if rc == 2 else ValueError("orc_gen_rmat arguments")
+    try:
+        off = np.ctypeslib.as_array(po, (n.value + 1,)).copy()
+        col = np.ctypeslib.as_array(pc, (max(1, m.value),))[:m.value].copy()
+        w = np.ctypeslib.as_array(pw, (max(1, m.value),))[:m.value].copy() if wmax else None
+    finally:
+        for p in (po, pc, pw):
+            if p:
+                lib().orc_free(ctypes.cast(p, ctypes.c_void_p))
+    return off, col, w
 
 
 # --- multithreaded restatement (timed CPU baseline) ------------------------

@@ -257,6 +257,16 @@ int orc_sssp_certificate(uint64_t n, const uint64_t *off, const uint32_t *col, c
         if (dist[u] == unreached_val) continue;
         for (uint64_t e = off[u]; e < off[u + 1]; e++) {
             uint32_t v = col[e];
+            if (v >= n) { /* a target outside the graph: no certificate */
+                rc = 5;
+                if (bad) *bad = u;
+                break;
+            }
+            if (w[e] == 0) { /* the tight-edge argument needs positive weights */
+                rc = 4;
+                if (bad) *bad = u;
+                break;
+            }
             uint64_t cand = (uint64_t)dist[u] + (uint64_t)w[e];
             uint64_t dv = dist[v] == unreached_val ? ~0ull : (uint64_t)dist[v];
             if (dv > cand) {

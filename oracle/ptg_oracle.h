@@ -70,17 +70,39 @@ void orc_mt_pagerank(uint64_t n, const uint64_t *off, const uint32_t *col, doubl
                      uint32_t iters, uint32_t threads, float *rank);
 
 /* Shortest-path certificate for graphs too large for Dijkstra here (the
- * out-of-core scale; the check streams the CSR once, O(n + m)): dist is the
- * exact SSSP answer from src (dist[src] = base, unreached = unreached_val)
- * iff dist[src] == base, no edge u->v from a reached u has
- * dist[v] > dist[u] + w (unreached v counts as infinite), and every reached
- * v != src has an in-edge with dist[v] == dist[u] + w (a tight edge; with
- * positive weights these form a shortest-path tree).  Returns 0 if the
- * certificate holds, else 1 + the first failed condition's index and, in
- * *bad, the vertex it failed at. */
+ * out-of-core scale; the check streams the CSR once, O(n + m)).  For edge
+ * weights >= 1, dist is the exact SSSP answer from src (dist[src] = base,
+ * unreached = unreached_val) iff dist[src] == base, no edge u->v from a
+ * reached u has dist[v] > dist[u] + w (unreached v counts as infinite), and
+ * every reached v != src has an in-edge from a reached u with
+ * dist[v] == dist[u] + w (a tight edge; following tight edges backwards
+ * strictly lowers dist, so it ends at src).  A zero weight on an edge out of
+ * a reached vertex voids that argument (a cycle of tight zero-weight edges
+ * could carry too-small distances), so it is reported instead of accepted.
+ * Returns 0 if the certificate holds, else: 1 dist[src] != base, 2 an edge
+ * still improves dist (bad = its target), 3 a reached vertex has no tight
+ * in-edge (bad = that vertex), 4 a zero weight out of a reached vertex, 5 a
+ * target >= n (bad = the edge's source for 4 and 5). */
 int orc_sssp_certificate(uint64_t n, const uint64_t *off, const uint32_t *col, const uint32_t *w,
                          uint32_t src, uint32_t base, uint32_t unreached_val, const uint32_t *dist,
                          uint64_t *bad);
+
+/* ---- at the benchmarked sizes (ptg_oracle_scale.cpp, std::thread) ------ */
+/* orc_sssp_certificate on `threads` cores (same codes). */
+int orc_mt_sssp_certificate(uint64_t n, const uint64_t *off, const uint32_t *col, const uint32_t *w,
+                            uint32_t src, uint32_t base, uint32_t unreached_val, const uint32_t *dist,
+                            uint32_t threads, uint64_t *bad);
+/* FP64 PageRank on a symmetric CSR as a pull over in-edges (= out-edges):
+ * the update of orc_pagerank_f64, on `threads` cores. */
+void orc_mt_pagerank_f64(uint64_t n, const uint64_t *off, const uint32_t *col, double d,
+                         uint32_t iters, uint32_t threads, double *rank);
+/* RMAT input of the benchmark (see ptg_oracle_scale.cpp for the draws);
+ * arrays are malloc'ed (free with orc_free; *w_out is NULL when wmax == 0).
+ * Returns 0, 1 for bad arguments, 2 when out of memory. */
+int orc_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+                 int symmetric, uint32_t wmin, uint32_t wmax, uint32_t threads, uint64_t *n_out,
+                 uint64_t *m_out, uint64_t **off_out, uint32_t **col_out, uint32_t **w_out);
+void orc_free(void *p);
 
 #ifdef __cplusplus
 }

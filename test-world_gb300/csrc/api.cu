@@ -424,7 +424,7 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
         g->m = csr->m;
         g->symmetric = (csr->flags & PTG_CSR_SYMMETRIC) != 0;
         g->weighted = csr->weight != nullptr || csr->edges_aos != nullptr;
-        g->off64 = csr->m >= (1ull << 32);
+        g->off64 = csr->m >= (1ull << 32) || (csr->flags & PTG_CSR_WIDE_OFFSETS) != 0;
         // the caller's offsets are read in place (no host copy): the device
         // validation pass checks that they never decrease
         const HostOffsets off{csr->offsets, csr->offset_type == PTG_OFFSETS_U64,

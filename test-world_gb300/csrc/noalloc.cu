@@ -72,6 +72,23 @@ struct DeviceSetup {
 std::mutex g_setup_mu;
 DeviceSetup g_setup[64];
 
+// Error bits of NaCtl::error: 1 a frontier append past the queue, 2 an edge
+// target >= n, 4 offsets that are not a CSR of m edges (off[0] != 0, a
+// decrease, or off[n] != m).  Any bit makes the call fail; the kernels below
+// stop at once when one is set, and never index outside their buffers.
+constexpr unsigned kErrTarget = 2u, kErrOffsets = 4u;
+
+// The caller's offsets, checked before any kernel reads edges through them:
+// off[0] == 0, off[i] <= off[i+1], off[n] == m.  Runs after k_na_init, which
+// clears the error word.
+__global__ void k_na_check(const uint32_t *off, uint32_t n, uint32_t m, NaCtl *ctl) {
+    bool bad = false;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        bad |= off[i] > off[i + 1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) bad |= off[0] != 0u || off[n] != m;
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(&ctl->error, kErrOffsets);
+}
+
 __global__ void k_na_init(uint32_t *level, uint32_t n, uint32_t src, uint32_t *q0, NaCtl *ctl) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         level[i] = i == src ? 1u : PTG_UNREACHED;
@@ -88,6 +105,7 @@ __global__ void k_na_init(uint32_t *level, uint32_t n, uint32_t src, uint32_t *q
 __global__ void __launch_bounds__(kBlock) k_na_scan_reduce(const uint32_t *q, const NaCtl *ctl,
                                                            const uint32_t *off,
                                                            unsigned long long *bsum) {
+    if (ctl->error) return;
     uint32_t F = ctl->F;
     uint32_t per = (F + gridDim.x - 1) / gridDim.x;
     uint32_t lo = min(F, blockIdx.x * per), hi = min(F, lo + per);
@@ -101,6 +119,7 @@ __global__ void __launch_bounds__(kBlock) k_na_scan_reduce(const uint32_t *q, co
 }
 
 __global__ void __launch_bounds__(kBlock) k_na_scan_bsums(unsigned long long *bsum, int nb, NaCtl *ctl) {
+    if (ctl->error) return;
     unsigned long long carry = 0;
     for (int base = 0; base < nb; base += kBlock) {
         int i = base + threadIdx.x;
@@ -116,6 +135,7 @@ __global__ void __launch_bounds__(kBlock) k_na_scan_write(const uint32_t *q, con
                                                           const uint32_t *off,
                                                           const unsigned long long *bsum, uint32_t *sc,
                                                           uint32_t *rs) {
+    if (ctl->error) return;
     uint32_t F = ctl->F;
     uint32_t per = (F + gridDim.x - 1) / gridDim.x;
     uint32_t lo = min(F, blockIdx.x * per), hi = min(F, lo + per);
@@ -144,10 +164,16 @@ __global__ void __launch_bounds__(kBlock) k_na_scan_write(const uint32_t *q, con
 __global__ void __launch_bounds__(kBlock) k_na_expand(const uint32_t *q, const uint32_t *sc,
                                                       const uint32_t *rs, const uint32_t *col,
                                                       uint32_t *level, uint32_t *q_next, NaCtl *ctl,
-                                                      uint32_t cap) {
+                                                      uint32_t cap, uint32_t m) {
     __shared__ uint32_t s_sc[kTile + 1];
     __shared__ uint32_t s_rs[kTile + 1];
-    __shared__ uint32_t s_r0, s_nrows;
+    __shared__ uint32_t s_r0, s_nrows, s_err;
+    // an error set before this launch stops the whole grid; one read per CTA,
+    // so every thread of a CTA takes the same branch (this kernel can set
+    // error bits itself while it runs)
+    if (threadIdx.x == 0) s_err = *(volatile unsigned *)&ctl->error;
+    __syncthreads();
+    if (s_err) return;
     uint32_t F = ctl->F;
     uint64_t E = ctl->E;
     uint32_t nd = ctl->level_val + 1u;
@@ -174,9 +200,14 @@ __global__ void __launch_bounds__(kBlock) k_na_expand(const uint32_t *q, const u
             uint64_t row = staged ? ptg::last_le(s_sc, 0, nrows, j) : ptg::last_le(sc, r0, r0 + nrows, j);
             uint32_t rsv = staged ? s_rs[row] : rs[row];
             uint32_t scv = staged ? s_sc[row] : sc[row];
-            uint32_t v = col[rsv + (uint32_t)(j - scv)];
+            uint64_t e = (uint64_t)rsv + (j - scv);
+            if (e >= m) {  // unreachable once the offsets passed k_na_check
+                atomicOr(&ctl->error, kErrOffsets);
+                continue;
+            }
+            uint32_t v = col[e];
             if (v >= cap) {  // target outside the graph: report, never write out of bounds
-                atomicOr(&ctl->error, 2u);
+                atomicOr(&ctl->error, kErrTarget);
                 continue;
             }
             if (level[v] == PTG_UNREACHED && atomicCAS(&level[v], PTG_UNREACHED, nd) == PTG_UNREACHED)
@@ -229,6 +260,7 @@ extern "C" ptg_status ptg_bfs_noalloc(const uint32_t *d_offsets, const uint32_t 
     const int sms = setup.sms > 0 ? setup.sms : 1;
 
     k_na_init<<<ptg::grid_for(n, kBlock, sms * 8), kBlock, 0, st>>>(d_levels, n, src, q[0], ctl);
+    k_na_check<<<ptg::grid_for(n, kBlock, sms * 8), kBlock, 0, st>>>(d_offsets, n, m, ctl);
     s = cuda_status(cudaGetLastError());
     if (s != PTG_OK) return s;
     uint32_t F = 1;
@@ -239,14 +271,14 @@ extern "C" ptg_status ptg_bfs_noalloc(const uint32_t *d_offsets, const uint32_t 
         k_na_scan_reduce<<<nb, kBlock, 0, st>>>(q[cur], ctl, d_offsets, bsum);
         k_na_scan_bsums<<<1, kBlock, 0, st>>>(bsum, nb, ctl);
         k_na_scan_write<<<nb, kBlock, 0, st>>>(q[cur], ctl, d_offsets, bsum, sc, rs);
-        k_na_expand<<<sms * 8, kBlock, 0, st>>>(q[cur], sc, rs, d_col, d_levels, q[cur ^ 1], ctl, n);
+        k_na_expand<<<sms * 8, kBlock, 0, st>>>(q[cur], sc, rs, d_col, d_levels, q[cur ^ 1], ctl, n, m);
         s = cuda_status(cudaGetLastError());
         if (s != PTG_OK) return s;
         NaCtl h{};
         s = cuda_status(cudaMemcpyAsync(&h, ctl, 32, cudaMemcpyDeviceToHost, st));
         if (s == PTG_OK) s = cuda_status(cudaStreamSynchronize(st));
         if (s != PTG_OK) return s;
-        if (h.error & 2u) return PTG_ERR_INVALID;  // an edge target is >= n
+        if (h.error & (kErrTarget | kErrOffsets)) return PTG_ERR_INVALID;  // not a CSR of n vertices, m edges
         if (h.error) return PTG_ERR_CUDA;
         F = h.next_tail;
         // next round: the new frontier becomes current, its append cursor restarts at zero

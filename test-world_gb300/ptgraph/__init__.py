@@ -25,7 +25,7 @@ PTG_OK, PTG_ERR_INVALID, PTG_ERR_OOM, PTG_ERR_CUDA, PTG_ERR_TIMEOUT = 0, 1, 2, 3
 PTG_ERR_UNSUPPORTED, PTG_ERR_NO_DEVICE, PTG_ERR_CANCELLED, PTG_ERR_BUSY = 5, 6, 7, 8
 PTG_OFFSETS_U32, PTG_OFFSETS_U64 = 0, 1
 PTG_FORM_SENTINEL, PTG_FORM_REFERENCE = 0, 1
-PTG_CSR_SYMMETRIC, PTG_CSR_HOST_PINNED = 1, 2
+PTG_CSR_SYMMETRIC, PTG_CSR_HOST_PINNED, PTG_CSR_WIDE_OFFSETS = 1, 2, 4
 PTG_RESIDENT_PREFIX, PTG_RESIDENT_NONE, PTG_RESIDENT_HOT, PTG_RESIDENT_HUBS = 0, 1, 2, 3
 PTG_OUT_DEVICE, PTG_LEVEL_ZERO_BASED, PTG_UNREACHED_MINUS1 = 1, 2, 4
 PTG_NO_DIRECTION_OPT, PTG_REFERENCE_SCHEDULE = 8, 16
@@ -365,8 +365,8 @@ class Ctx:
         return out
 
     def graph(self, offsets, col, weight=None, symmetric=False, form=PTG_FORM_SENTINEL,
-              edges_aos=None, config=None, pinned=False):
-        return Graph(self, offsets, col, weight, symmetric, form, edges_aos, config, pinned)
+              edges_aos=None, config=None, pinned=False, wide_offsets=False):
+        return Graph(self, offsets, col, weight, symmetric, form, edges_aos, config, pinned, wide_offsets)
 
     def cc_batch(self, vtx_begin, offsets, col, stats=None):
         vb = np.ascontiguousarray(vtx_begin, dtype=np.uint64)
@@ -389,7 +389,7 @@ class Graph:
     """An uploaded CSR (resident in HBM, or resident prefix + streamed partitions)."""
 
     def __init__(self, ctx, offsets, col, weight=None, symmetric=False, form=PTG_FORM_SENTINEL,
-                 edges_aos=None, config=None, pinned=False):
+                 edges_aos=None, config=None, pinned=False, wide_offsets=False):
         self.ctx = ctx
         off = np.ascontiguousarray(offsets)
         if off.dtype not in (np.uint32, np.uint64):
@@ -408,7 +408,8 @@ class Graph:
         c.col = _ptr(self._col) if self._col is not None and m else None
         c.weight = _ptr(self._w) if self._w is not None and m else None
         c.edges_aos = _ptr(self._aos) if self._aos is not None and m else None
-        c.flags = (PTG_CSR_SYMMETRIC if symmetric else 0) | (PTG_CSR_HOST_PINNED if pinned else 0)
+        c.flags = ((PTG_CSR_SYMMETRIC if symmetric else 0) | (PTG_CSR_HOST_PINNED if pinned else 0) |
+                   (PTG_CSR_WIDE_OFFSETS if wide_offsets else 0))
         if m == 0:
             # a graph without edges still needs a valid (unused) edge pointer
             self._col = np.zeros(1, dtype=np.uint32)

@@ -9,7 +9,7 @@ ssspCaculateIn{Share,Opt}, ccCaculateIn{Share,Opt}) is run, the out-of-core
 ones with a small edge budget so their overload/gather path is exercised; the
 script asserts that all variants agree and stores one result per algorithm.
 
-    python tests/golden/make_golden.py [REF_DIR]
+    python tests/golden/make_golden.py REF_DIR   (or PTG_REFERENCE_DIR=... python ...)
 
 The fixtures hold the graphs themselves, so they do not depend on the
 generator staying the same.
@@ -127,7 +127,9 @@ def run_all(name, off, col, w, sources, symmetric):
 
 
 def main():
-    ref_dir = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/ptGraph"
+    ref_dir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PTG_REFERENCE_DIR", "")
+    if not ref_dir:
+        sys.exit("usage: make_golden.py <reference ptGraph dir> (or set PTG_REFERENCE_DIR)")
     O.build()
     O.build_ref(ref_dir)
     import ptgraph

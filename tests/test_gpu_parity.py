@@ -34,17 +34,26 @@ def configs(ptg, m):
     }
 
 
+# "_u64": the same placement with 64-bit offsets on the device (the width
+# graphs of 2^32+ edges get), forced on these small graphs
+CFGNAMES = ["resident", "resident_grouped", "ooc_prefix", "ooc_none_3buf",
+            "resident_u64", "resident_grouped_u64", "ooc_prefix_u64"]
+
+
 @pytest.mark.parametrize("path", GOLD, ids=IDS)
-@pytest.mark.parametrize("cfgname", ["resident", "resident_grouped", "ooc_prefix", "ooc_none_3buf"])
+@pytest.mark.parametrize("cfgname", CFGNAMES)
 def test_bfs_sssp_cc_match_reference(ptg, ctx, ctx_grouped, path, cfgname):
     g = load(path)
     sym = bool(g["symmetric"][0])
-    c = ctx_grouped if cfgname == "resident_grouped" else ctx
-    cfg = configs(ptg, g["col"].size).get(cfgname)
-    G = c.graph(g["off"], g["col"], g["w"], symmetric=sym, config=cfg)
+    wide = cfgname.endswith("_u64")
+    place = cfgname[:-4] if wide else cfgname
+    c = ctx_grouped if place == "resident_grouped" else ctx
+    cfg = configs(ptg, g["col"].size).get(place)
+    G = c.graph(g["off"], g["col"], g["w"], symmetric=sym, config=cfg, wide_offsets=wide)
     info = G.info()
-    assert info["degree_grouped"] == (cfgname == "resident_grouped" and sym and g["col"].size > 0)
-    if cfgname.startswith("ooc") and g["col"].size > 16:
+    assert info["degree_grouped"] == (place == "resident_grouped" and sym and g["col"].size > 0)
+    assert info["offsets_u64"] == int(wide)
+    if place.startswith("ooc") and g["col"].size > 16:
         assert info["out_of_core"] == 1
     for i, s in enumerate(g["sources"]):
         s = int(s)
@@ -108,11 +117,13 @@ def test_drop_in_out_of_core_config(ptg):
         ptg.compat.set_partition_config(None)
 
 
+@pytest.mark.parametrize("wide", [False, True], ids=["u32off", "u64off"])
 @pytest.mark.parametrize("name", ["rmat8_sym", "rmat10_sym", "rmat12_sym", "path10", "star20",
                                   "two_comp_isolated", "single_vertex", "no_edges"])
-def test_pagerank_within_tolerance(ptg, ctx, oracle, name):
+def test_pagerank_within_tolerance(ptg, ctx, oracle, name, wide):
     g = load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
-    G = ctx.graph(g["off"], g["col"], symmetric=True)
+    G = ctx.graph(g["off"], g["col"], symmetric=True, wide_offsets=wide)
+    assert G.info()["offsets_u64"] == int(wide)
     r = G.pagerank().astype(np.float64)
     ref = oracle.pagerank(g["off"], g["col"])
     rel = np.abs(r - ref) / ref
@@ -140,10 +151,11 @@ def test_config1_rmat16_bfs_from_vertex0(ptg, ctx, oracle):
     assert (out == lv).all()
 
 
-@pytest.mark.parametrize("scale", [14, 18])
-def test_rmat_weighted_suite_vs_oracle(ptg, ctx, oracle, scale):
+@pytest.mark.parametrize("scale,wide", [(14, False), (18, False), (14, True), (18, True)])
+def test_rmat_weighted_suite_vs_oracle(ptg, ctx, oracle, scale, wide):
     off, col, w = ptg.gen_rmat(scale, 16, seed=2, symmetric=True, wmin=1, wmax=63)
-    G = ctx.graph(off, col, w, symmetric=True)
+    G = ctx.graph(off, col, w, symmetric=True, wide_offsets=wide)
+    assert G.info()["offsets_u64"] == int(wide)
     deg = np.diff(off.astype(np.int64))
     rng = np.random.default_rng(scale)
     srcs = rng.choice(np.nonzero(deg)[0], 4, replace=False)
@@ -157,11 +169,12 @@ def test_rmat_weighted_suite_vs_oracle(ptg, ctx, oracle, scale):
     assert (np.abs(r - ref) / ref).max() < PR_RTOL
 
 
-def test_directed_rmat_out_of_core_vs_oracle(ptg, ctx, oracle):
+@pytest.mark.parametrize("wide", [False, True], ids=["u32off", "u64off"])
+def test_directed_rmat_out_of_core_vs_oracle(ptg, ctx, oracle, wide):
     off, col, w = ptg.gen_rmat(14, 16, seed=3, symmetric=False, wmin=1, wmax=63)
     cfg = ptg.partition_config(partition_bytes=1 << 16, device_budget_bytes=1 << 18, force_out_of_core=1)
-    G = ctx.graph(off, col, w, symmetric=False, config=cfg)
-    assert G.info()["out_of_core"] == 1
+    G = ctx.graph(off, col, w, symmetric=False, config=cfg, wide_offsets=wide)
+    assert G.info()["out_of_core"] == 1 and G.info()["offsets_u64"] == int(wide)
     st = {}
     d = G.sssp(0, stats=st)
     assert (d == oracle.sssp(off, col, w, 0)).all()
@@ -170,16 +183,18 @@ def test_directed_rmat_out_of_core_vs_oracle(ptg, ctx, oracle):
     assert (G.cc() == oracle.cc(off, col)).all()
 
 
-def test_streamed_sssp_certificate_rmat20(ptg, ctx, oracle):
+@pytest.mark.parametrize("wide", [False, True], ids=["u32off", "u64off"])
+def test_streamed_sssp_certificate_rmat20(ptg, ctx, oracle, wide):
     """The check used where Dijkstra on the host is out of reach (the
     out-of-core scale): a one-pass shortest-path certificate over the CSR,
     here on a directed RMAT-20 with three quarters of its edges streamed in
-    4 MiB partitions, from several sources."""
+    4 MiB partitions, from several sources; with 64-bit offsets on the device
+    too, the width the out-of-core scale (34 B edges) needs."""
     off, col, w = ptg.gen_rmat(20, 16, seed=3, symmetric=False, wmin=1, wmax=63)
     edge_bytes = col.size * 8
     cfg = ptg.partition_config(partition_bytes=4 << 20, device_budget_bytes=edge_bytes // 4, force_out_of_core=1)
-    G = ctx.graph(off, col, w, symmetric=False, config=cfg)
-    assert G.info()["out_of_core"] == 1
+    G = ctx.graph(off, col, w, symmetric=False, config=cfg, wide_offsets=wide)
+    assert G.info()["out_of_core"] == 1 and G.info()["offsets_u64"] == int(wide)
     deg = np.diff(off.astype(np.int64))
     for s in [0] + [int(x) for x in np.random.default_rng(8).choice(np.nonzero(deg)[0], 2, replace=False)]:
         st = {}
@@ -233,11 +248,11 @@ def test_msbfs_equals_single_source(ptg, ctx):
         assert (ss[i] == G.sssp(int(s))).all()
 
 
-@pytest.mark.parametrize("symmetric", [True, False])
-def test_multi_source_groups_vs_oracle(ptg, ctx, oracle, symmetric):
+@pytest.mark.parametrize("symmetric,wide", [(True, False), (False, False), (True, True), (False, True)])
+def test_multi_source_groups_vs_oracle(ptg, ctx, oracle, symmetric, wide):
     """Several 64-source groups (130 sources), both push and pull levels."""
     off, col, w = ptg.gen_rmat(14, 16, seed=6, symmetric=symmetric, wmin=1, wmax=63)
-    G = ctx.graph(off, col, w, symmetric=symmetric)
+    G = ctx.graph(off, col, w, symmetric=symmetric, wide_offsets=wide)
     rng = np.random.default_rng(14)
     srcs = rng.integers(0, off.size - 1, 130).astype(np.uint32)
     ms = G.msbfs(srcs)
@@ -274,12 +289,13 @@ def _sym_csr(n, edges):
     return np.cumsum(off).astype(np.uint64), both[:, 1].astype(np.uint32)
 
 
+@pytest.mark.parametrize("wide", [False, True], ids=["u32off", "u64off"])
 @pytest.mark.parametrize("name", ["rmat10_sym", "rmat12_sym", "star20", "two_comp_isolated", "single_vertex",
                                   "no_edges", "path10"])
-def test_ppr_batch_vs_oracle(ptg, ctx, oracle, name):
+def test_ppr_batch_vs_oracle(ptg, ctx, oracle, name, wide):
     g = load(os.path.join(os.path.dirname(__file__), "golden", name + ".npz"))
     n = g["off"].size - 1
-    G = ctx.graph(g["off"], g["col"], symmetric=True)
+    G = ctx.graph(g["off"], g["col"], symmetric=True, wide_offsets=wide)
     srcs = np.unique(np.concatenate([g["sources"], [0, n - 1]])).astype(np.uint32)
     pb = G.ppr_batch(srcs)
     for i, s in enumerate(srcs):
@@ -291,7 +307,8 @@ def test_ppr_batch_vs_oracle(ptg, ctx, oracle, name):
         assert np.array_equal(pb[i].view(np.uint32), G.ppr(int(s)).view(np.uint32)), (name, int(s))
 
 
-def test_ppr_batch_long_rows_and_independence(ptg, ctx, oracle):
+@pytest.mark.parametrize("wide", [False, True], ids=["u32off", "u64off"])
+def test_ppr_batch_long_rows_and_independence(ptg, ctx, oracle, wide):
     """Rows longer than one warp's chunk (hubs of 5000 and 9000 edges), 40 sources
     (five passes); every row is bit-identical to the single-source PPR, and so the
     same alone and in any pass."""
@@ -300,7 +317,7 @@ def test_ppr_batch_long_rows_and_independence(ptg, ctx, oracle):
     edges = [(0, v) for v in range(1, 5001)] + [(1, v) for v in range(3000, 12000)]
     edges += list(map(tuple, rng.integers(0, n, (30000, 2))))
     off, col = _sym_csr(n, edges)
-    G = ctx.graph(off, col, symmetric=True)
+    G = ctx.graph(off, col, symmetric=True, wide_offsets=wide)
     srcs = rng.choice(n, 40, replace=False).astype(np.uint32)
     srcs[0], srcs[1] = 0, 1
     pb = G.ppr_batch(srcs)
@@ -318,14 +335,15 @@ def test_ppr_batch_long_rows_and_independence(ptg, ctx, oracle):
     assert np.array_equal(shuffled[::-1].view(np.uint32), pb.view(np.uint32))
 
 
-def test_hot_partition_cache(ptg, ctx, oracle):
+@pytest.mark.parametrize("wide", [False, True], ids=["u32off", "u64off"])
+def test_hot_partition_cache(ptg, ctx, oracle, wide):
     """PTG_RESIDENT_HOT: no static prefix; partitions promoted by visit counts stay in
     device slots across traversals, so a repeated search streams fewer bytes."""
     off, col, w = ptg.gen_rmat(14, 16, seed=3, symmetric=False, wmin=1, wmax=63)
     pb = max(64, (col.size * 8 // 16) // 8 * 8)  # about 16 partitions of weighted edges
     cfg = ptg.partition_config(partition_bytes=pb, device_budget_bytes=pb * 9, force_out_of_core=1,
                                n_staging_buffers=2, resident_policy=ptg.PTG_RESIDENT_HOT, hot_threshold=1)
-    G = ctx.graph(off, col, w, symmetric=False, config=cfg)
+    G = ctx.graph(off, col, w, symmetric=False, config=cfg, wide_offsets=wide)
     info = G.info()
     assert info["out_of_core"] == 1 and info["resident_partitions"] == 0
     assert (G.bfs(0) == oracle.bfs(off, col, 0, method="queue")).all()  # fills slots with columns only
@@ -335,7 +353,7 @@ def test_hot_partition_cache(ptg, ctx, oracle):
     assert (G.sssp(0, stats=s2) == ref).all()
     cfg_none = ptg.partition_config(partition_bytes=pb, device_budget_bytes=pb * 9, force_out_of_core=1,
                                     n_staging_buffers=2, resident_policy=ptg.PTG_RESIDENT_NONE)
-    N = ctx.graph(off, col, w, symmetric=False, config=cfg_none)
+    N = ctx.graph(off, col, w, symmetric=False, config=cfg_none, wide_offsets=wide)
     assert (N.sssp(0, stats=sn) == ref).all()
     # the order of improvements within a level varies, so compare with streaming everything
     assert s2["partitions_cached"] > 0 and s2["link_bytes"] < 0.8 * sn["link_bytes"]
