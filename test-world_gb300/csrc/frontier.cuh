@@ -14,13 +14,30 @@
 namespace ptg {
 namespace {
 
-// Degree of frontier entry i, clipped to the resident edge prefix.
+// Degrees (clipped to the resident edge prefix) and row starts of the queue
+// entries i0 .. i0+kScanItems-1 (those below hi): a thread's kScanItems consecutive entries, with all their
+// offset loads in flight together.
+constexpr int kScanItems = 4;
 template <class OffT>
-__device__ __forceinline__ OffT clipped_degree(const OffT *off, uint32_t u, OffT clip, OffT &start) {
-    OffT b = off[u], e = off[u + 1];
-    start = b;
-    if (e > clip) e = clip;
-    return e > b ? (OffT)(e - b) : (OffT)0;
+__device__ __forceinline__ unsigned long long scan_items(const uint32_t *q, const OffT *off, OffT clip, uint64_t i0,
+                                                         uint64_t hi, OffT (&d)[kScanItems], OffT (&st)[kScanItems]) {
+    uint32_t u[kScanItems];
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) u[k] = i0 + k < hi ? q[i0 + k] : 0u;
+    OffT e[kScanItems];
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        st[k] = i0 + k < hi ? off[u[k]] : (OffT)0;
+        e[k] = i0 + k < hi ? off[u[k] + 1] : (OffT)0;
+    }
+    unsigned long long t = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        OffT ce = e[k] > clip ? clip : e[k];
+        d[k] = ce > st[k] ? (OffT)(ce - st[k]) : (OffT)0;
+        t += (unsigned long long)d[k];
+    }
+    return t;
 }
 
 // Pass 1 of the frontier degree scan: per-CTA sums over contiguous slices.
@@ -32,9 +49,9 @@ __global__ void __launch_bounds__(kBlock) k_scan_reduce(const uint32_t *q, const
     uint64_t per = (F + gridDim.x - 1) / gridDim.x;
     uint64_t lo = min(F, (uint64_t)blockIdx.x * per), hi = min(F, lo + per);
     unsigned long long s = 0;
-    for (uint64_t i = lo + threadIdx.x; i < hi; i += kBlock) {
-        OffT st;
-        s += clipped_degree(off, q[i], clip, st);
+    for (uint64_t i = lo + threadIdx.x * kScanItems; i < hi; i += kBlock * kScanItems) {
+        OffT d[kScanItems], st[kScanItems];
+        s += scan_items(q, off, clip, i, hi, d, st);
     }
     s = block_reduce_sum(s);
     if (threadIdx.x == 0) bsum[blockIdx.x] = s;
@@ -68,15 +85,18 @@ __global__ void __launch_bounds__(kBlock) k_scan_write(const uint32_t *q, const 
     uint64_t per = (F + gridDim.x - 1) / gridDim.x;
     uint64_t lo = min(F, (uint64_t)blockIdx.x * per), hi = min(F, lo + per);
     unsigned long long run = bsum[blockIdx.x];
-    for (uint64_t base = lo; base < hi; base += kBlock) {
-        uint64_t i = base + threadIdx.x;
-        OffT d = 0, st = 0;
-        if (i < hi) d = clipped_degree(off, q[i], clip, st);
+    for (uint64_t base = lo; base < hi; base += kBlock * kScanItems) {
+        const uint64_t i0 = base + threadIdx.x * kScanItems;
+        OffT d[kScanItems], st[kScanItems];
         unsigned long long tot;
-        unsigned long long ex = block_exclusive_scan((unsigned long long)d, tot);
-        if (i < hi) {
-            sc[i] = (OffT)(run + ex);
-            rs[i] = st;
+        unsigned long long ex = block_exclusive_scan(scan_items(q, off, clip, i0, hi, d, st), tot);
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            if (i0 + k < hi) {
+                sc[i0 + k] = (OffT)(run + ex);
+                rs[i0 + k] = st[k];
+            }
+            ex += (unsigned long long)d[k];
         }
         run += tot;
     }
@@ -91,15 +111,18 @@ __global__ void __launch_bounds__(kBlock) k_scan_small(const uint32_t *q, TravCt
                                                        OffT clip, OffT *sc, OffT *rs) {
     uint64_t F = ctl->F;
     unsigned long long run = 0;
-    for (uint64_t base = 0; base < F; base += kBlock) {
-        uint64_t i = base + threadIdx.x;
-        OffT d = 0, st = 0;
-        if (i < F) d = clipped_degree(off, q[i], clip, st);
+    for (uint64_t base = 0; base < F; base += kBlock * kScanItems) {
+        const uint64_t i0 = base + threadIdx.x * kScanItems;
+        OffT d[kScanItems], st[kScanItems];
         unsigned long long tot;
-        unsigned long long ex = block_exclusive_scan((unsigned long long)d, tot);
-        if (i < F) {
-            sc[i] = (OffT)(run + ex);
-            rs[i] = st;
+        unsigned long long ex = block_exclusive_scan(scan_items(q, off, clip, i0, F, d, st), tot);
+#pragma unroll
+        for (int k = 0; k < kScanItems; k++) {
+            if (i0 + k < F) {
+                sc[i0 + k] = (OffT)(run + ex);
+                rs[i0 + k] = st[k];
+            }
+            ex += (unsigned long long)d[k];
         }
         run += tot;
     }

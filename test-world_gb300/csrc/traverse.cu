@@ -137,6 +137,24 @@ __device__ __forceinline__ void relax_probe(const PushTargets &t, uint32_t v, ui
 // bitmap (BFS) and take near vertices out of the far pile (SSSP).  With off
 // given it also sums the new frontier's degrees into ctl->next_E, which the
 // host reads with the frontier size and uses for the next push/pull choice.
+constexpr int kCompactBatch = 4;
+
+// Vertex of set bit r of a warp's 32 bitmap words (word wd0 + lane in lane
+// `lane`, pre = inclusive popcount prefix over the lanes); every lane calls
+// it, each with its own r < the warp's total.
+__device__ __forceinline__ uint32_t warp_bit_vertex(uint32_t word, uint32_t pre, uint64_t wd0, uint32_t r) {
+    uint32_t lo = 0;  // first lane whose inclusive prefix exceeds r
+#pragma unroll
+    for (uint32_t step = 16; step > 0; step >>= 1) {
+        const uint32_t x = __shfl_sync(0xffffffffu, pre, lo + step - 1);
+        if (x <= r) lo += step;
+    }
+    lo = min(lo, 31u);
+    const uint32_t w = __shfl_sync(0xffffffffu, word, lo);
+    const uint32_t ex = __shfl_sync(0xffffffffu, pre, lo) - __popc(w);
+    return (uint32_t)((wd0 + lo) * 32 + __fns(w, 0, (int)(r - ex) + 1));
+}
+
 template <class OffT>
 __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t *bm, uint64_t words, uint32_t *q,
                                                     TravCtl *ctl, uint32_t *vis, uint32_t *far_bm,
@@ -172,14 +190,33 @@ __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t *bm, uint64_t
             s_base = run ? atomicAdd(&ctl->next_tail, run) : 0u;
         }
         __syncthreads();
-        uint32_t pos = s_base + s_warp[wid] + pre - cnt;
+        const uint32_t wbase = s_base + s_warp[wid];
+        const uint32_t wtotal = __shfl_sync(0xffffffffu, pre, 31);
         __syncthreads();  // s_warp / s_base are rewritten by the next step
-        while (word) {
-            int b = __ffs(word) - 1;
-            word &= word - 1;
-            uint32_t v = (uint32_t)(wd * 32 + b);
-            q[pos++] = v;
-            if (off) degsum += (unsigned long long)(off[v + 1] - off[v]);
+        // the warp's set bits in vertex order, 32 at a time (bit r to lane
+        // r % 32): coalesced queue stores, and the degree loads of
+        // kCompactBatch rounds in flight together (a lane walking its own
+        // word waited on one offset load per bit of a dense word)
+        const uint64_t wd0 = (c0 + wid) * 32;
+        for (uint32_t r0 = 0; r0 < wtotal; r0 += 32 * kCompactBatch) {  // warp-uniform bound
+            uint32_t v[kCompactBatch];
+#pragma unroll
+            for (int u = 0; u < kCompactBatch; u++) {
+                const uint32_t r = r0 + 32 * u + lane;
+                v[u] = warp_bit_vertex(word, pre, wd0, r < wtotal ? r : 0u);
+                if (r < wtotal) q[wbase + r] = v[u];
+            }
+            if (off) {
+                OffT b[kCompactBatch], e[kCompactBatch];
+#pragma unroll
+                for (int u = 0; u < kCompactBatch; u++) {
+                    const bool ok = r0 + 32 * u + lane < wtotal;
+                    b[u] = ok ? off[v[u]] : (OffT)0;
+                    e[u] = ok ? off[v[u] + 1] : (OffT)0;
+                }
+#pragma unroll
+                for (int u = 0; u < kCompactBatch; u++) degsum += (unsigned long long)(e[u] - b[u]);
+            }
         }
     }
     if (off) {
@@ -336,11 +373,12 @@ __global__ void __launch_bounds__(kBlock, 8) k_bottom_up(uint64_t n, const OffT 
     const uint64_t chunks = (words + kBuWords - 1) / kBuWords;
     while (true) {
         // warps take chunks from a shared counter: chunk costs vary a lot
-        uint64_t c = 0;
-        if (lane == 0) c = atomicAdd(&t.ctl->bu_next, 1u);
-        c = __shfl_sync(0xffffffffu, c, 0);
-        if (c >= chunks) break;
-        uint64_t wd = c * kBuWords + lane;
+        uint64_t chunk = 0;
+        if (lane == 0) chunk = atomicAdd(&t.ctl->bu_next, 1u);
+        chunk = __shfl_sync(0xffffffffu, chunk, 0);
+        if (chunk >= chunks) break;
+        const uint64_t cw0 = chunk * kBuWords;  // first bitmap word of the chunk
+        uint64_t wd = cw0 + lane;
         bool mine = lane < (unsigned)kBuWords && wd < words;
         uint32_t visw = 0, cand = 0;
         if (mine) {
@@ -363,21 +401,44 @@ __global__ void __launch_bounds__(kBlock, 8) k_bottom_up(uint64_t n, const OffT 
         }
         s_found[wid][lane] = 0;
         __syncwarp();
-        for (uint32_t i = lane; i < total; i += 32) {
-            uint32_t v = s_list[wid][i];
-            OffT b = off[v], e = off[v + 1];
-            bool found = false;
-            for (OffT k = b; k < e && !found; k += 4) {
-                uint32_t c0 = col[k];
-                uint32_t c1 = k + 1 < e ? col[k + 1] : c0;
-                uint32_t c2 = k + 2 < e ? col[k + 2] : c0;
-                uint32_t c3 = k + 3 < e ? col[k + 3] : c0;
-                found = bit_test(bm_cur, c0) | bit_test(bm_cur, c1) | bit_test(bm_cur, c2) |
-                        bit_test(bm_cur, c3);
+        // two candidates per lane at a time: their offset loads, then their
+        // first four neighbours' column loads, then those neighbours' bit
+        // tests are in flight together (rows list their highest-degree
+        // neighbours first on a degree-grouped graph, so most candidates are
+        // settled by the first four); the rest of a row is walked after
+        for (uint32_t i = lane; i < total; i += 64) {
+            const bool has2 = i + 32 < total;
+            const uint32_t v0 = s_list[wid][i], v1 = has2 ? s_list[wid][i + 32] : v0;
+            const OffT b0 = off[v0], e0 = off[v0 + 1];
+            const OffT b1 = has2 ? off[v1] : (OffT)0, e1 = has2 ? off[v1 + 1] : (OffT)0;
+            uint32_t c[8];
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                c[j] = b0 + (OffT)j < e0 ? col[b0 + j] : PTG_UNREACHED;
+                c[4 + j] = b1 + (OffT)j < e1 ? col[b1 + j] : PTG_UNREACHED;
             }
-            if (found) {
-                atomicOr(&s_found[wid][(v >> 5) - (uint32_t)(c * kBuWords)], 1u << (v & 31u));
-                t.value[value_slot(t, v)] = newval;
+            bool f[2] = {false, false};
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+                if (c[j] != PTG_UNREACHED) f[j >> 2] |= bit_test(bm_cur, c[j]);
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                if (h == 1 && !has2) break;
+                const uint32_t v = h ? v1 : v0;
+                const OffT e = h ? e1 : e0;
+                bool found = f[h];
+                for (OffT k = (h ? b1 : b0) + 4; k < e && !found; k += 4) {
+                    uint32_t c0 = col[k];
+                    uint32_t c1 = k + 1 < e ? col[k + 1] : c0;
+                    uint32_t c2 = k + 2 < e ? col[k + 2] : c0;
+                    uint32_t c3 = k + 3 < e ? col[k + 3] : c0;
+                    found = bit_test(bm_cur, c0) | bit_test(bm_cur, c1) | bit_test(bm_cur, c2) |
+                            bit_test(bm_cur, c3);
+                }
+                if (found) {
+                    atomicOr(&s_found[wid][(v >> 5) - (uint32_t)(cw0)], 1u << (v & 31u));
+                    t.value[value_slot(t, v)] = newval;
+                }
             }
         }
         __syncwarp();
