@@ -235,8 +235,9 @@ __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t *bm, uint64_t
 // loads go through L1 (the 32 threads of a warp cover 1 KB of consecutive
 // edges) with an L2 evict-first hint.
 constexpr int kExpandPerThread = kTile / kBlock;
+constexpr int kStageRows = (kTile + 2 + kBlock - 1) / kBlock;  // rows (+1 sentinel) a thread stages
 template <class OffT, int MODE>
-__global__ void __launch_bounds__(kBlock) k_expand(const uint32_t *q, const OffT *sc, const OffT *rs,
+__global__ void __launch_bounds__(kBlock, 4) k_expand(const uint32_t *q, const OffT *sc, const OffT *rs,
                                                    const uint32_t *tr, const uint32_t *col,
                                                    const uint32_t *w, PushTargets t) {
     __shared__ OffT s_sc[kTile + 2];
@@ -254,11 +255,30 @@ __global__ void __launch_bounds__(kBlock) k_expand(const uint32_t *q, const OffT
         uint64_t r0 = tr[tile];
         uint32_t nrows = (uint32_t)((uint64_t)tr[tile + 1] - r0 + 1);
         if (nrows <= (uint32_t)kTile + 1) {
-            for (uint32_t k = threadIdx.x; k <= nrows; k += kBlock) {
-                s_sc[k] = sc[r0 + k];
+            // stage the tile's rows (scan values, row starts, source values);
+            // a thread's row loads go out together, then its value loads (a
+            // tile of short rows has up to 2049 rows, 9 per thread, and one
+            // round trip per row and load kind left it latency-bound)
+            OffT scv[kStageRows], rsv[kStageRows];
+            uint32_t qv[kStageRows];
+#pragma unroll
+            for (int i = 0; i < kStageRows; i++) {
+                const uint32_t k = threadIdx.x + i * kBlock;
+                scv[i] = k <= nrows ? sc[r0 + k] : (OffT)0;
+                rsv[i] = k < nrows ? rs[r0 + k] : (OffT)0;
+                qv[i] = k < nrows ? q[r0 + k] : 0u;
+            }
+            uint32_t vv[kStageRows];
+#pragma unroll
+            for (int i = 0; i < kStageRows; i++)
+                vv[i] = threadIdx.x + i * kBlock < nrows ? t.value[value_slot(t, qv[i])] : 0u;
+#pragma unroll
+            for (int i = 0; i < kStageRows; i++) {
+                const uint32_t k = threadIdx.x + i * kBlock;
+                if (k <= nrows) s_sc[k] = scv[i];
                 if (k < nrows) {
-                    s_rs[k] = rs[r0 + k];
-                    s_val[k] = t.value[value_slot(t, q[r0 + k])];
+                    s_rs[k] = rsv[i];
+                    s_val[k] = vv[i];
                 }
             }
             __syncthreads();
