@@ -60,6 +60,9 @@ def parse():
     p.add_argument("--sssp-sources", type=int, default=4)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the batched and served workloads that follow the suite (their summaries are the "
+                        "line's batch / serve keys)")
     p.add_argument("--no-parity", action="store_true",
                    help="skip the check of the suite's results against the oracle (run outside the timed region)")
     p.add_argument("--tuning", default="",
@@ -71,10 +74,13 @@ def parse():
                         "serve: a Poisson stream of BFS/SSSP/PPR requests through the server; "
                         "ooc: SSSP from vertex 0 on a directed RMAT graph streamed from pinned host memory")
     p.add_argument("--ooc-scale", type=int, default=27)
+    p.add_argument("--ooc-runs", default="all_streamed,half_resident,half_hot_cache")
     p.add_argument("--serve-scale", type=int, default=26)
     p.add_argument("--serve-uploads", type=int, default=16)
     p.add_argument("--serve-requests", type=int, default=4000)
     p.add_argument("--serve-rate", type=float, default=2000.0)
+    p.add_argument("--serve-low-rate", type=float, default=150.0)
+    p.add_argument("--serve-low-requests", type=int, default=600)
     p.add_argument("--serve-lanes", type=int, default=2)
     p.add_argument("--serve-schedule", type=int, default=0, help="0: oldest first, 1: response ratio")
     p.add_argument("--plain-sample", type=int, default=240)
@@ -86,7 +92,7 @@ def parse():
     return p.parse_args()
 
 
-def batch_workload(args):
+def batch_workload(args, emit=True):
     """Config 4: batched queries against the plain one-at-a-time path (same results checked)."""
     import torch
     import ptgraph
@@ -126,10 +132,12 @@ def batch_workload(args):
                 pass
         plain_ms *= k / sample
         # identical results on a sample of rows
+        checked = 0
         for i in range(0, k, max(1, k // 8)):
             single(int(srcs[i]), flags=ptgraph.PTG_OUT_DEVICE, out=one)
             assert torch.equal(out[i], one), name
-        res[name] = {"batched_ms": batched_ms, "plain_ms_extrapolated": plain_ms,
+            checked += 1
+        res[name] = {"batched_ms": batched_ms, "plain_ms_extrapolated": plain_ms, "identical_rows_checked": checked,
                      "batched_queries_per_s": k / batched_ms * 1e3, "plain_queries_per_s": k / plain_ms * 1e3,
                      "speedup": plain_ms / batched_ms, "plain_sample": sample,
                      "rounds": pst.get("iterations"), "edges_relaxed": pst.get("edges_relaxed"),
@@ -161,23 +169,30 @@ def batch_workload(args):
                        "batched_ms": batch_ms, "plain_ms_extrapolated": plain_ms,
                        "batched_graphs_per_s": args.er_graphs / batch_ms * 1e3,
                        "plain_graphs_per_s": args.er_graphs / plain_ms * 1e3, "speedup": plain_ms / batch_ms,
-                       "plain_sample": psample, "gen_s": gen_s,
+                       "plain_sample": psample, "identical_graphs_checked": psample, "gen_s": gen_s,
                        "note": "device time of the kernels; plain = one ptg_cc launch sequence per graph"}
-    print(json.dumps({"workload": "batched", "metric": "batched_queries_per_s", "results": res}))
+    G.close()
+    ctx.close()
+    if emit:
+        print(json.dumps({"workload": "batched", "metric": "batched_queries_per_s", "results": res}))
+    return res
 
 
-def serve_workload(args):
-    """Serving: a seeded Poisson stream (rate --serve-rate) of BFS 50% / SSSP 30% /
-    PPR 20% (FP32, 20 iterations) requests over a resident RMAT graph of scale
-    --serve-scale and --serve-uploads uploaded RMAT graphs of scales 10..20, all
-    admitted through the server's memory budget.  Each request picks its graph
-    uniformly and a random non-isolated source; results are copied to pinned host
-    buffers.  Latency = completion - scheduled arrival.  The plain method (one
-    query at a time through ptg_bfs/ptg_sssp/ptg_ppr, host outputs) is timed on
-    the first --plain-sample requests of the same stream; its throughput is the
-    sample's count / summed service time, and its latencies follow from a FIFO
-    single-server queue (Lindley's recursion) fed the same arrivals with the
-    measured service times of each request's (graph, kind) class."""
+def serve_workload(args, emit=True):
+    """Serving: a seeded Poisson stream of BFS 50% / SSSP 30% / PPR 20% (FP32,
+    20 iterations) requests over a resident RMAT graph of scale --serve-scale
+    and --serve-uploads uploaded RMAT graphs of scales 10..20, all admitted
+    through the server's memory budget.  Each request picks its graph
+    uniformly and a random non-isolated source; results are copied to pinned
+    host buffers.  Latency = completion - scheduled arrival.  The stream runs
+    at --serve-rate (2000/s, above what the GPU serves: capacity and queueing)
+    and again, --serve-low-requests long, at --serve-low-rate (below the plain
+    path's capacity: latency of service, not of queueing).  The plain method
+    (one query at a time through ptg_bfs/ptg_sssp/ptg_ppr, host outputs) is
+    timed on the first --plain-sample requests of the stream; its throughput is
+    the sample's count / summed service time, and its latencies follow from a
+    FIFO single-server queue (Lindley's recursion) fed the same arrivals with
+    the measured service times of each request's (graph, kind) class."""
     import queue
     import torch
     import ptgraph
@@ -192,11 +207,6 @@ def serve_workload(args):
         graphs.append(ptgraph.gen_rmat(sc, 16, 0.57, 0.19, 0.19, seed=100 + i, symmetric=True, wmin=1, wmax=63))
     gen_s = time.time() - t0
     nz = [np.nonzero(np.diff(off.astype(np.int64)))[0].astype(np.uint32) for off, _, _ in graphs]
-    N = args.serve_requests
-    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, N))
-    kinds = rng.choice(3, N, p=[0.5, 0.3, 0.2])
-    gidx = rng.integers(0, len(graphs), N)
-    srcs = np.array([nz[g][rng.integers(nz[g].size)] for g in gidx], dtype=np.uint32)
 
     srv = ptgraph.Server(ctx, lanes=args.serve_lanes, schedule=args.serve_schedule)
     t0 = time.time()
@@ -211,66 +221,81 @@ def serve_workload(args):
         for _ in range(64 if n > (1 << 22) else 128):
             q.put(torch.empty(n, dtype=torch.int32, pin_memory=True))
         pools.append(q)
-    keep = {}  # copies of a few results for the identity check against the plain path
-    done_t = np.zeros(N)
-    sub_t = np.zeros(N)
-    lat_srv = np.zeros(N)
-    work = queue.Queue()
-
-    def waiter():
-        while True:
-            item = work.get()
-            if item is None:
-                return
-            i, rid, buf = item
-            _, lat = srv.wait(rid)
-            lat_srv[i] = lat * 1e-6
-            if i < 48:
-                keep[i] = buf.numpy().copy()
-            pools[gidx[i]].put(buf)
-
-    waiters = [threading.Thread(target=waiter) for _ in range(8)]
-    for t in waiters:
-        t.start()
-    start = time.perf_counter()
-    for i in range(N):
-        delay = start + arrivals[i] - time.perf_counter()
-        if delay > 0:
-            time.sleep(delay)
-        buf = pools[gidx[i]].get()
-        sub_t[i] = time.perf_counter() - start
-        rid = srv.submit(gids[gidx[i]], int(kinds[i]), int(srcs[i]), out=buf)
-        work.put((i, rid, buf))
-    for _ in waiters:
-        work.put(None)
-    for t in waiters:
-        t.join()
-    srv_stats = srv.stats()
-    srv.close()
-    lat = (sub_t - arrivals) + lat_srv
-    done_t = sub_t + lat_srv
-    makespan = done_t.max() - arrivals[0]
     names = ["bfs", "sssp", "ppr"]
-    big = gidx == 0
 
     def pct(x):
         return {"p50_ms": float(np.percentile(x, 50) * 1e3), "p99_ms": float(np.percentile(x, 99) * 1e3),
                 "count": int(x.size)} if x.size else None
 
-    res = {"requests": N, "offered_rate": args.serve_rate, "qps": N / makespan, "makespan_s": makespan,
-           **{k: v for k, v in pct(lat).items() if k != "count"},
-           "by_kind": {names[k]: pct(lat[kinds == k]) for k in range(3)},
-           "resident_graph": pct(lat[big]), "uploaded_graphs": pct(lat[~big]),
+    def stream(rate, N, keep_first):
+        """One Poisson stream through the server; returns its request table and latencies."""
+        arrivals = np.cumsum(rng.exponential(1.0 / rate, N))
+        kinds = rng.choice(3, N, p=[0.5, 0.3, 0.2])
+        gidx = rng.integers(0, len(graphs), N)
+        srcs = np.array([nz[g][rng.integers(nz[g].size)] for g in gidx], dtype=np.uint32)
+        keep = {}
+        sub_t = np.zeros(N)
+        lat_srv = np.zeros(N)
+        work = queue.Queue()
+
+        def waiter():
+            while True:
+                item = work.get()
+                if item is None:
+                    return
+                i, rid, buf = item
+                _, lat = srv.wait(rid)
+                lat_srv[i] = lat * 1e-6
+                if i < keep_first:
+                    keep[i] = buf.numpy().copy()
+                pools[gidx[i]].put(buf)
+
+        waiters = [threading.Thread(target=waiter) for _ in range(8)]
+        for t in waiters:
+            t.start()
+        start = time.perf_counter()
+        for i in range(N):
+            delay = start + arrivals[i] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            buf = pools[gidx[i]].get()
+            sub_t[i] = time.perf_counter() - start
+            rid = srv.submit(gids[gidx[i]], int(kinds[i]), int(srcs[i]), out=buf)
+            work.put((i, rid, buf))
+        for _ in waiters:
+            work.put(None)
+        for t in waiters:
+            t.join()
+        lat = (sub_t - arrivals) + lat_srv
+        makespan = (sub_t + lat_srv).max() - arrivals[0]
+        return {"arrivals": arrivals, "kinds": kinds, "gidx": gidx, "srcs": srcs, "keep": keep, "lat": lat,
+                "makespan": makespan}
+
+    def summary(r, rate):
+        lat, kinds, big = r["lat"], r["kinds"], r["gidx"] == 0
+        return {"requests": int(lat.size), "offered_rate": rate, "qps": lat.size / r["makespan"],
+                "makespan_s": r["makespan"], **{k: v for k, v in pct(lat).items() if k != "count"},
+                "by_kind": {names[k]: pct(lat[kinds == k]) for k in range(3)},
+                "resident_graph": pct(lat[big]), "uploaded_graphs": pct(lat[~big])}
+
+    sat = stream(args.serve_rate, args.serve_requests, 48)
+    low = stream(args.serve_low_rate, args.serve_low_requests, 48)
+    srv_stats = srv.stats()
+    srv.close()
+    res = {"saturated": summary(sat, args.serve_rate), "sub_saturated": summary(low, args.serve_low_rate),
            "server": {k: srv_stats[k] for k in ("batches", "max_batch_seen", "failed", "launches",
                                                  "resident_graphs", "streamed_graphs", "budget_bytes",
                                                  "committed_bytes", "busy_ms", "fused_requests",
                                                  "single_requests", "fused_batches", "fused_ms", "single_ms")},
-           "lanes": args.serve_lanes, "schedule": ["oldest", "response_ratio"][args.serve_schedule], "graphs": {"resident_scale": args.serve_scale, "upload_scales": scales,
-                                                 "admitted_resident": [bool(r) for _, r in up]},
+           "lanes": args.serve_lanes, "schedule": ["oldest", "response_ratio"][args.serve_schedule],
+           "graphs": {"resident_scale": args.serve_scale, "upload_scales": scales,
+                      "admitted_resident": [bool(r) for _, r in up]},
            "gen_s": gen_s, "upload_s": upload_s}
-    # plain: one query at a time, same requests, host outputs
+    # plain: one query at a time, the saturated stream's first requests, host outputs
     G = {}
-    svc = np.zeros(min(args.plain_sample, N))
+    kinds, gidx, srcs = sat["kinds"], sat["gidx"], sat["srcs"]
+    svc = np.zeros(min(args.plain_sample, kinds.size))
+    identical = 0
     for i in range(svc.size):
         g = int(gidx[i])
         if g not in G:
@@ -286,31 +311,38 @@ def serve_workload(args):
         else:
             G[g].ppr(int(srcs[i]), out=o.view(np.float32))
         svc[i] = time.perf_counter() - t
-        if i in keep:
-            assert np.array_equal(keep[i], o) if kinds[i] != 2 else \
-                np.allclose(keep[i].view(np.float32), o.view(np.float32), rtol=2e-6, atol=0), i
+        if i in sat["keep"]:
+            assert np.array_equal(sat["keep"][i], o) if kinds[i] != 2 else \
+                np.allclose(sat["keep"][i].view(np.float32), o.view(np.float32), rtol=2e-6, atol=0), i
+            identical += 1
     for h in G.values():
         h.close()
-    cls_mean = {}
+    ctx.close()
+    cls = {}
     for i in range(svc.size):
-        cls_mean.setdefault((int(gidx[i]), int(kinds[i])), []).append(svc[i])
-    cls_mean = {k: float(np.mean(v)) for k, v in cls_mean.items()}
+        cls.setdefault((int(gidx[i]), int(kinds[i])), []).append(svc[i])
+    cls = {k: float(np.mean(v)) for k, v in cls.items()}
     kind_mean = {k: float(np.mean(svc[kinds[:svc.size] == k])) for k in range(3)}
-    est = np.array([cls_mean.get((int(gidx[i]), int(kinds[i])), kind_mean[int(kinds[i])]) for i in range(N)])
-    fin = np.zeros(N)
-    free_at = 0.0
-    for i in range(N):
-        st_i = max(arrivals[i], free_at)
-        free_at = st_i + est[i]
-        fin[i] = free_at
-    plat = fin - arrivals
     plain_qps = svc.size / svc.sum()
+
+    def plain_queue(r):
+        est = np.array([cls.get((int(g), int(k)), kind_mean[int(k)]) for g, k in zip(r["gidx"], r["kinds"])])
+        fin = np.zeros(est.size)
+        free_at = 0.0
+        for i in range(est.size):
+            free_at = max(r["arrivals"][i], free_at) + est[i]
+            fin[i] = free_at
+        plat = fin - r["arrivals"]
+        return {"p50_ms_simulated": float(np.percentile(plat, 50) * 1e3),
+                "p99_ms_simulated": float(np.percentile(plat, 99) * 1e3)}
+
     res["plain"] = {"qps": plain_qps, "sample": int(svc.size), "mean_service_ms": float(svc.mean() * 1e3),
-                    "p50_ms_simulated": float(np.percentile(plat, 50) * 1e3),
-                    "p99_ms_simulated": float(np.percentile(plat, 99) * 1e3)}
-    res["speedup_qps"] = res["qps"] / plain_qps
-    res["identical_results_checked"] = len([i for i in keep if i < svc.size])
-    print(json.dumps({"workload": "serve", "metric": "served_queries_per_s", "results": res}))
+                    "saturated": plain_queue(sat), "sub_saturated": plain_queue(low)}
+    res["speedup_qps"] = res["saturated"]["qps"] / plain_qps
+    res["identical_results_checked"] = identical
+    if emit:
+        print(json.dumps({"workload": "serve", "metric": "served_queries_per_s", "results": res}))
+    return res
 
 
 def pinned_h2d_gbs(nbytes=2 << 30, reps=5):
@@ -335,37 +367,50 @@ def pinned_h2d_gbs(nbytes=2 << 30, reps=5):
 def ooc_workload(args):
     """Out-of-core SSSP (the reference's ssspCaculateInOpt query): directed RMAT,
     edge factor 16, a/b/c/d .57/.19/.19/.05, seed 3, u32 weights [1,63], source
-    vertex 0, the edge arrays in host memory and streamed through HBM in 256 MB
-    partitions.  Three placements: every partition streamed (the link alone),
-    half of the edges resident as a static prefix with the rest streamed, and
-    the same budget as a cache of hot partitions (each after one warm-up search).  Reports the copy-stream
-    rate (link bytes / time the copy stream was busy) and the link's share of the
-    run against the measured pinned host->device rate, plus GTEPS of the search."""
+    vertex 0, the edge arrays generated straight into pinned host memory and
+    streamed through HBM in the tuned partition size (32 MiB).  Placements
+    (--ooc-runs): every partition streamed (the link alone), half of the edges
+    resident as a static prefix with the rest streamed, and the same budget as
+    a cache of hot partitions (each after one warm-up search).  Reports the
+    copy-stream rate (link bytes / time the copy stream was busy) and the link's
+    share of the run against the measured pinned host->device rate, GTEPS, the
+    offset width the graph got (64-bit from 2^32 edges on), and whether the
+    distances pass the one-pass shortest-path certificate on the host."""
     import ptgraph
+    from oracle import oracle as O
     local = int(os.environ.get("LOCAL_RANK", "0"))
     ctx = make_ctx(args, local)
+    threads = os.cpu_count() or 1
     t0 = time.time()
-    off, col, w = ptgraph.gen_rmat(args.ooc_scale, 16, 0.57, 0.19, 0.19, seed=3, symmetric=False, wmin=1, wmax=63)
+    H = ptgraph.gen_rmat_host(args.ooc_scale, 16, 0.57, 0.19, 0.19, seed=3, symmetric=False, wmin=1, wmax=63,
+                              pinned=True)
+    off, col, w = H.offsets, H.col, H.weight
     gen_s = time.time() - t0
     n, m = off.size - 1, col.size
     peak = pinned_h2d_gbs()
-    res = {"graph": {"scale": args.ooc_scale, "n": n, "m": m, "edge_bytes": 8 * m, "directed": True},
+    deg = np.diff(off.astype(np.int64))
+    res = {"graph": {"scale": args.ooc_scale, "n": n, "m": m, "edge_bytes": 8 * m, "directed": True,
+                     "host_arrays": "pinned at generation"},
            "pinned_h2d_gbs": peak, "gen_s": gen_s, "runs": {}}
     edge_bytes = 8 * m
-    for name, kw in (("all_streamed", dict(resident_policy=ptgraph.PTG_RESIDENT_NONE, device_budget_bytes=1 << 30)),
-                     ("half_resident", dict(device_budget_bytes=edge_bytes // 2)),
-                     ("half_hot_cache", dict(resident_policy=ptgraph.PTG_RESIDENT_HOT,
-                                             device_budget_bytes=edge_bytes // 2))):
-        cfg = ptgraph.partition_config(force_out_of_core=1, n_staging_buffers=3, **kw)
+    placements = {"all_streamed": dict(resident_policy=ptgraph.PTG_RESIDENT_NONE, device_budget_bytes=1 << 30),
+                  "half_resident": dict(device_budget_bytes=edge_bytes // 2),
+                  "half_hot_cache": dict(resident_policy=ptgraph.PTG_RESIDENT_HOT, device_budget_bytes=edge_bytes // 2)}
+    for name in args.ooc_runs.split(","):
+        cfg = ptgraph.partition_config(force_out_of_core=1, n_staging_buffers=3, **placements[name])
         t0 = time.time()
-        G = ctx.graph(off, col, w, symmetric=False, config=cfg)
+        G = ctx.graph(off, col, w, symmetric=False, config=cfg, pinned=True)
         up_s = time.time() - t0
         info = G.info()
-        G.sssp(0)  # warm-up (page registration, workspace)
+        G.sssp(0)  # warm-up (workspace; the hot cache's first fill)
         st = {}
         d = G.sssp(0, stats=st)
-        reached = int((d != 0xFFFFFFFF).sum())
-        comp_edges = int(np.diff(off.astype(np.int64))[d != 0xFFFFFFFF].sum())
+        reached_mask = d != 0xFFFFFFFF
+        reached = int(reached_mask.sum())
+        comp_edges = int(deg[reached_mask].sum())
+        t0 = time.time()
+        ok, rc, bad = O.mt_sssp_certificate(off, col, w, 0, d, threads)
+        cert_s = time.time() - t0
         ms = st["device_ms"]
         res["runs"][name] = {
             "device_ms": ms, "rounds": st["iterations"], "reached": reached, "edges_in_component": comp_edges,
@@ -377,10 +422,15 @@ def ooc_workload(args):
             "link_share_of_run": st["link_ms"] / ms if ms else None,
             "link_gbs_over_run": st["link_bytes"] / (ms * 1e-3) / 1e9,
             "partitions": info["partitions"], "resident_partitions": info["resident_partitions"],
+            "offsets_u64": info["offsets_u64"],
             "partitions_streamed": st["partitions_streamed"], "partitions_skipped": st["partitions_skipped"],
             "partitions_cached": st["partitions_cached"],
-            "redundancy_vs_settle_once": st["link_bytes"] / max(1, 8 * comp_edges), "upload_s": up_s}
+            "redundancy_vs_settle_once": st["link_bytes"] / max(1, 8 * comp_edges), "upload_s": up_s,
+            "certificate": {"ok": bool(ok), "code": rc, "vertex": bad, "check_s": round(cert_s, 1),
+                            "threads": threads}}
         G.close()
+        del d, reached_mask
+    H.close()
     print(json.dumps({"workload": "ooc", "metric": "ooc_sssp_link_gbs", "results": res}))
 
 
@@ -697,6 +747,12 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(off, col, w, sources, deg, args)
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        G.close()
+        del dev
+        torch.cuda.empty_cache()
+        extras = run_extras(args, local)
     if rank == 0:
         line = {"metric": "suite_gteps", "value": value, "unit": "GTEPS", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_per_step, "wall_ms_per_step": 1e3 * wall / args.steps,
@@ -705,8 +761,48 @@ def main():
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches // args.steps,
                 "clocks": clock_info, "parity": parity, "algorithms": algs,
                 "kernel_profile_ms": {k: [c, round(t, 4)] for k, (c, t) in prof.items()},
-                "graph": {"n": n, "m": m, "gen_s": round(gen_s, 2)}}
+                "graph": {"n": n, "m": m, "gen_s": round(gen_s, 2)}, **extras}
         print(json.dumps(line))
+
+
+def run_extras(args, local):
+    """The batched (config 4) and served (config 5) workloads after the suite,
+    as compact summaries for the suite's line, each with the clocks seen while
+    it ran."""
+    out = {}
+    clocks = ClockSampler(local)
+    clocks.start()
+    b = batch_workload(args, emit=False)
+    out["batch"] = {
+        "config": "MS-BFS / MS-SSSP from %d seeded sources on RMAT scale %d (ef 16, seed 4, weights [1,63]); "
+                  "CC over %d Erdos-Renyi graphs, n log-uniform in [1K, 1M], average degree 8"
+                  % (args.batch_sources, b["graph"]["scale"], args.er_graphs),
+        "plain": "the same queries one at a time (ptg_bfs / ptg_sssp / ptg_cc), device time, extrapolated "
+                 "from a sample of 64 sources / 128 graphs",
+        "msbfs": {k: b["bfs"][k] for k in ("batched_ms", "plain_ms_extrapolated", "speedup", "identical_rows_checked")},
+        "mssssp": {k: b["sssp"][k] for k in ("batched_ms", "plain_ms_extrapolated", "speedup",
+                                              "identical_rows_checked")},
+        "cc_batch": {k: b["cc_batch"][k] for k in ("batched_ms", "plain_ms_extrapolated", "speedup",
+                                                   "identical_graphs_checked")}}
+    out["batch"]["clocks"] = clocks.stop()
+    clocks = ClockSampler(local)
+    clocks.start()
+    r = serve_workload(args, emit=False)
+    sat, low = r["saturated"], r["sub_saturated"]
+    out["serve"] = {
+        "config": "Poisson BFS 50%% / SSSP 30%% / PPR 20%% over a resident RMAT-%d and %d uploads of scale 10-20, "
+                  "%d lanes" % (args.serve_scale, args.serve_uploads, args.serve_lanes),
+        "saturated": {"offered_rate": sat["offered_rate"], "requests": sat["requests"], "qps": sat["qps"],
+                      "plain_qps": r["plain"]["qps"], "speedup_qps": r["speedup_qps"], "p50_ms": sat["p50_ms"],
+                      "p99_ms": sat["p99_ms"], "plain_p50_ms_simulated": r["plain"]["saturated"]["p50_ms_simulated"],
+                      "plain_p99_ms_simulated": r["plain"]["saturated"]["p99_ms_simulated"]},
+        "sub_saturated": {"offered_rate": low["offered_rate"], "requests": low["requests"], "qps": low["qps"],
+                          "p50_ms": low["p50_ms"], "p99_ms": low["p99_ms"],
+                          "plain_p50_ms_simulated": r["plain"]["sub_saturated"]["p50_ms_simulated"],
+                          "plain_p99_ms_simulated": r["plain"]["sub_saturated"]["p99_ms_simulated"]},
+        "identical_results_checked": r["identical_results_checked"]}
+    out["serve"]["clocks"] = clocks.stop()
+    return out
 
 
 def peaks():
@@ -869,7 +965,7 @@ def e2e_measure(ctx, off32, col, w, sources, args, deg, step_edges, n, m):
     for _ in range(min(2, args.warmup)):
         step()
     torch.cuda.synchronize()
-    k = max(1, min(3, args.steps))
+    k = max(1, min(5, args.steps))
     t0 = time.perf_counter()
     for _ in range(k):
         step()

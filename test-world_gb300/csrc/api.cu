@@ -10,6 +10,7 @@
 #include <unistd.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -86,6 +87,21 @@ __global__ void k_aos_to_soa(const ptg_edge_w *e, uint64_t m, uint32_t *col, uin
         col[i] = x.to;
         w[i] = x.weight;
     }
+}
+
+// fn(lo, hi) over [0, count) cut into one range per host core.
+template <class F>
+void host_parallel(uint64_t count, F &&fn) {
+    unsigned T = std::thread::hardware_concurrency();
+    if (T == 0) T = 1;
+    if (count < (1ull << 20) || T == 1) {
+        fn(0, count);
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (unsigned t = 0; t < T; t++)
+        pool.emplace_back([&fn, count, t, T] { fn(count * t / T, count * (t + 1) / T); });
+    for (auto &th : pool) th.join();
 }
 
 size_t host_page() {
@@ -545,24 +561,39 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
             uint64_t e0 = RE, ne = g->m - RE;
             const uint32_t *hc = csr->col, *hw = csr->weight;
             bool own = csr->col == nullptr;  // AoS input: build owned pinned SoA copies
+            // the streamed targets are checked here (the resident ones were
+            // checked on the device), on all host cores: at 10^10 edges one
+            // thread takes tens of seconds
+            std::atomic<bool> bad_target{false};
             if (!own) {
-                for (uint64_t j = e0; j < g->m; j++)
-                    PTG_REQUIRE(hc[j] < g->n, PTG_ERR_INVALID, "an edge target is >= n");
+                host_parallel(g->m - e0, [&](uint64_t lo, uint64_t hi) {
+                    bool bad = false;
+                    for (uint64_t j = e0 + lo; j < e0 + hi; j++) bad |= hc[j] >= g->n;
+                    if (bad) bad_target = true;
+                });
             }
             if (own) {
                 g->own_col.ensure(g->m * 4);
                 g->own_w.ensure(g->m * 4);
-                for (uint64_t j = 0; j < g->m; j++) {
-                    PTG_REQUIRE(csr->edges_aos[j].to < g->n, PTG_ERR_INVALID, "an edge target is >= n");
-                    g->own_col.as<uint32_t>()[j] = csr->edges_aos[j].to;
-                    g->own_w.as<uint32_t>()[j] = csr->edges_aos[j].weight;
-                }
-                g->h_col = g->own_col.as<uint32_t>();
-                g->h_w = g->own_w.as<uint32_t>();
-            } else if (csr->flags & PTG_CSR_HOST_PINNED) {
+                uint32_t *oc = g->own_col.as<uint32_t>(), *ow = g->own_w.as<uint32_t>();
+                const ptg_edge_w *aos = csr->edges_aos;
+                host_parallel(g->m, [&](uint64_t lo, uint64_t hi) {
+                    bool bad = false;
+                    for (uint64_t j = lo; j < hi; j++) {
+                        bad |= aos[j].to >= g->n;
+                        oc[j] = aos[j].to;
+                        ow[j] = aos[j].weight;
+                    }
+                    if (bad) bad_target = true;
+                });
+                g->h_col = oc;
+                g->h_w = ow;
+            }
+            PTG_REQUIRE(!bad_target, PTG_ERR_INVALID, "an edge target is >= n");
+            if (!own && (csr->flags & PTG_CSR_HOST_PINNED)) {
                 g->h_col = hc;
                 g->h_w = hw;
-            } else {
+            } else if (!own) {
                 // register the caller's streamed range (page-aligned)
                 size_t pg = host_page();
                 auto reg = [&](const uint32_t *base, PinnedBuf &fallback, const uint32_t *&dst, int which) {

@@ -89,85 +89,6 @@ void free_bytes(void *p, int pinned) {
     else std::free(p);
 }
 
-// Build a deduplicated CSR from packed (u << 32 | v) keys.  Threads own
-// vertex ranges and each scans all keys, so no atomics and no per-thread
-// histograms of size n are needed.
-ptg_status build_csr(std::vector<uint64_t> &keys, uint64_t n, uint32_t T, int pinned, uint64_t wseed,
-                     uint32_t wmin, uint32_t wmax, ptg_host_csr *out) {
-    std::vector<uint64_t> deg(n + 1, 0);
-    auto range_of = [&](uint32_t t, uint64_t &lo, uint64_t &hi) {
-        lo = n * t / T;
-        hi = n * (t + 1) / T;
-    };
-    const uint64_t K = keys.size();
-    parallel(T, [&](uint32_t t, uint32_t) {
-        uint64_t lo, hi;
-        range_of(t, lo, hi);
-        for (uint64_t k = 0; k < K; k++) {
-            uint64_t u = keys[k] >> 32, v = keys[k] & 0xffffffffu;
-            if (u >= lo && u < hi && u != v) deg[u]++;
-        }
-    });
-    std::vector<uint64_t> start(n + 1, 0);
-    for (uint64_t v = 0; v < n; v++) start[v + 1] = start[v] + deg[v];
-    std::vector<uint32_t> tmp(std::max<uint64_t>(1, start[n]));
-    parallel(T, [&](uint32_t t, uint32_t) {
-        uint64_t lo, hi;
-        range_of(t, lo, hi);
-        std::vector<uint64_t> cur(start.begin() + lo, start.begin() + hi);
-        for (uint64_t k = 0; k < K; k++) {
-            uint64_t u = keys[k] >> 32, v = keys[k] & 0xffffffffu;
-            if (u >= lo && u < hi && u != v) tmp[cur[u - lo]++] = (uint32_t)v;
-        }
-    });
-    keys.clear();
-    keys.shrink_to_fit();
-    // sort + dedup each adjacency list (dynamic chunks: hubs are uneven)
-    std::atomic<uint64_t> next{0};
-    const uint64_t chunk = 4096;
-    parallel(T, [&](uint32_t, uint32_t) {
-        for (;;) {
-            uint64_t c0 = next.fetch_add(chunk);
-            if (c0 >= n) break;
-            uint64_t c1 = std::min(n, c0 + chunk);
-            for (uint64_t u = c0; u < c1; u++) {
-                uint32_t *b = tmp.data() + start[u], *e = tmp.data() + start[u + 1];
-                std::sort(b, e);
-                deg[u] = (uint64_t)(std::unique(b, e) - b);
-            }
-        }
-    });
-    uint64_t m = 0;
-    for (uint64_t v = 0; v < n; v++) m += deg[v];
-    out->n = n;
-    out->m = m;
-    out->pinned = pinned ? 1 : 0;
-    out->offsets = (uint64_t *)alloc_bytes((n + 1) * 8, pinned);
-    out->col = (uint32_t *)alloc_bytes(m * 4, pinned);
-    out->weight = wmax ? (uint32_t *)alloc_bytes(m * 4, pinned) : nullptr;
-    if (!out->offsets || !out->col || (wmax && !out->weight)) {
-        free_bytes(out->offsets, pinned);
-        free_bytes(out->col, pinned);
-        free_bytes(out->weight, pinned);
-        std::memset(out, 0, sizeof(*out));
-        return PTG_ERR_OOM;
-    }
-    out->offsets[0] = 0;
-    for (uint64_t v = 0; v < n; v++) out->offsets[v + 1] = out->offsets[v] + deg[v];
-    parallel(T, [&](uint32_t t, uint32_t) {
-        uint64_t lo, hi;
-        range_of(t, lo, hi);
-        for (uint64_t u = lo; u < hi; u++) {
-            uint64_t o = out->offsets[u], d = deg[u];
-            std::memcpy(out->col + o, tmp.data() + start[u], d * 4);
-            if (wmax)
-                for (uint64_t k = 0; k < d; k++)
-                    out->weight[o + k] = edge_weight(wseed, (uint32_t)u, out->col[o + k], wmin, wmax);
-        }
-    });
-    return PTG_OK;
-}
-
 uint32_t default_threads(uint32_t t) {
     if (t) return t;
     unsigned h = std::thread::hardware_concurrency();
@@ -185,32 +106,110 @@ ptg_status ptg_gen_rmat(uint32_t scale, uint32_t edge_factor, double a, double b
     if (a < 0 || b < 0 || c < 0 || a + b + c > 1.0) return PTG_ERR_INVALID;
     if (wmax && wmin > wmax) return PTG_ERR_INVALID;
     std::memset(out, 0, sizeof(*out));
-    uint32_t T = default_threads(threads);
-    uint64_t n = 1ull << scale;
-    uint64_t E = (uint64_t)edge_factor << scale;
+    const uint32_t T = default_threads(threads);
+    const uint64_t n = 1ull << scale;
+    const uint64_t E = (uint64_t)edge_factor << scale;
     auto thr = [](double p) {
         double x = p * 4294967296.0;
         return x >= 4294967295.0 ? 0xFFFFFFFFu : (uint32_t)x;
     };
-    uint32_t ta = thr(a), tab = thr(a + b), tabc = thr(a + b + c);
-    uint64_t mseed = splitmix64(seed);
+    const uint32_t ta = thr(a), tab = thr(a + b), tabc = thr(a + b + c);
+    const uint64_t mseed = splitmix64(seed);
+    uint64_t *offsets = nullptr;
+    uint32_t *col = nullptr, *wt = nullptr;
     try {
-        std::vector<uint64_t> keys(symmetric ? 2 * E : E);
+        // Two passes over the same counter-based draws, so no edge list is
+        // held: the first counts each row's slots, the second scatters the
+        // targets into the rows' slots of the output array itself; rows are
+        // then sorted and deduplicated in place and slid down to close the
+        // gaps the duplicates left.  Peak memory: the output arrays plus 12
+        // bytes per vertex.
+        std::vector<std::atomic<uint32_t>> cnt(n);
         parallel(T, [&](uint32_t t, uint32_t nt) {
-            uint64_t lo = E * t / nt, hi = E * (t + 1) / nt;
-            for (uint64_t i = lo; i < hi; i++) {
+            for (uint64_t v = n * t / nt, hi = n * (t + 1) / nt; v < hi; v++) cnt[v].store(0, std::memory_order_relaxed);
+        });
+        parallel(T, [&](uint32_t t, uint32_t nt) {
+            for (uint64_t i = E * t / nt, hi = E * (t + 1) / nt; i < hi; i++) {
                 uint32_t u, v;
                 rmat_edge(mseed, i, scale, ta, tab, tabc, u, v);
-                if (symmetric) {
-                    keys[2 * i] = ((uint64_t)u << 32) | v;
-                    keys[2 * i + 1] = ((uint64_t)v << 32) | u;
-                } else {
-                    keys[i] = ((uint64_t)u << 32) | v;
+                if (u == v) continue;
+                cnt[u].fetch_add(1, std::memory_order_relaxed);
+                if (symmetric) cnt[v].fetch_add(1, std::memory_order_relaxed);
+            }
+        });
+        offsets = (uint64_t *)alloc_bytes((n + 1) * 8, pinned);
+        if (!offsets) return PTG_ERR_OOM;
+        offsets[0] = 0;
+        for (uint64_t v = 0; v < n; v++) offsets[v + 1] = offsets[v] + cnt[v].load(std::memory_order_relaxed);
+        const uint64_t slots = offsets[n];
+        col = (uint32_t *)alloc_bytes(slots * 4, pinned);
+        if (!col) {
+            free_bytes(offsets, pinned);
+            return PTG_ERR_OOM;
+        }
+        parallel(T, [&](uint32_t t, uint32_t nt) {
+            for (uint64_t v = n * t / nt, hi = n * (t + 1) / nt; v < hi; v++) cnt[v].store(0, std::memory_order_relaxed);
+        });
+        parallel(T, [&](uint32_t t, uint32_t nt) {
+            for (uint64_t i = E * t / nt, hi = E * (t + 1) / nt; i < hi; i++) {
+                uint32_t u, v;
+                rmat_edge(mseed, i, scale, ta, tab, tabc, u, v);
+                if (u == v) continue;
+                col[offsets[u] + cnt[u].fetch_add(1, std::memory_order_relaxed)] = v;
+                if (symmetric) col[offsets[v] + cnt[v].fetch_add(1, std::memory_order_relaxed)] = u;
+            }
+        });
+        // sort + dedup each row in its slots (dynamic chunks: hubs are uneven);
+        // cnt[u] becomes the row's deduplicated length
+        std::atomic<uint64_t> next{0};
+        const uint64_t chunk = 4096;
+        parallel(T, [&](uint32_t, uint32_t) {
+            for (;;) {
+                uint64_t c0 = next.fetch_add(chunk);
+                if (c0 >= n) break;
+                for (uint64_t u = c0, c1 = std::min(n, c0 + chunk); u < c1; u++) {
+                    uint32_t *p = col + offsets[u], *q = col + offsets[u + 1];
+                    std::sort(p, q);
+                    cnt[u].store((uint32_t)(std::unique(p, q) - p), std::memory_order_relaxed);
                 }
             }
         });
-        return build_csr(keys, n, T, pinned, splitmix64(seed ^ 0x5eed5eedull), wmin, wmax, out);
+        // close the gaps: row u slides down to its final start, which is at
+        // or before its slot start, in increasing u (no row overwrites one
+        // not yet moved)
+        uint64_t m = 0;
+        for (uint64_t u = 0; u < n; u++) {
+            const uint64_t d = cnt[u].load(std::memory_order_relaxed), from = offsets[u];
+            offsets[u] = m;
+            if (from != m && d) std::memmove(col + m, col + from, d * 4);
+            m += d;
+        }
+        offsets[n] = m;
+        if (wmax) {
+            wt = (uint32_t *)alloc_bytes(std::max<uint64_t>(m, 1) * 4, pinned);
+            if (!wt) {
+                free_bytes(offsets, pinned);
+                free_bytes(col, pinned);
+                return PTG_ERR_OOM;
+            }
+            const uint64_t wseed = splitmix64(seed ^ 0x5eed5eedull);
+            parallel(T, [&](uint32_t t, uint32_t nt) {
+                for (uint64_t u = n * t / nt, hi = n * (t + 1) / nt; u < hi; u++)
+                    for (uint64_t e = offsets[u]; e < offsets[u + 1]; e++)
+                        wt[e] = edge_weight(wseed, (uint32_t)u, col[e], wmin, wmax);
+            });
+        }
+        out->n = n;
+        out->m = m;
+        out->pinned = pinned ? 1 : 0;
+        out->offsets = offsets;
+        out->col = col;
+        out->weight = wt;
+        return PTG_OK;
     } catch (const std::bad_alloc &) {
+        free_bytes(offsets, pinned);
+        free_bytes(col, pinned);
+        free_bytes(wt, pinned);
         return PTG_ERR_OOM;
     }
 }

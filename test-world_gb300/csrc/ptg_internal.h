@@ -317,6 +317,8 @@ enum TravKind { TRAV_BFS = 0, TRAV_SSSP = 1, TRAV_CCPROP = 2 };
 
 void run_traversal(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value, uint32_t flags,
                    uint32_t delta, uint32_t max_iters, RunResult &rr);
+// Mean resident edge weight of a weighted graph (measured once per graph).
+double graph_mean_weight(ptg_graph *g);
 void run_cc_hook(ptg_graph *g, uint32_t *d_label, RunResult &rr);
 void run_pagerank(ptg_graph *g, bool personalized, uint32_t src, double damping, uint32_t iters,
                   float *d_rank, RunResult &rr);

@@ -1013,6 +1013,11 @@ void trav_prepare_graph(ptg_graph *g) {
     measure_mean_weight(g);
 }
 
+double graph_mean_weight(ptg_graph *g) {
+    measure_mean_weight(g);
+    return g->mean_weight;
+}
+
 void run_traversal(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value, uint32_t flags,
                    uint32_t delta, uint32_t max_iters, RunResult &rr) {
     uint32_t *val = d_value;

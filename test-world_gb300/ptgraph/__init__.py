@@ -649,6 +649,42 @@ def gen_rmat(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1, symmetric=Tr
     return _take(hc, wmax > 0)
 
 
+class HostGraph:
+    """A host CSR owned by the library, seen as numpy arrays without a copy
+    (offsets u64 n+1, col u32, weight u32 or None); pinned when asked, so an
+    out-of-core graph streams from it as it is (ctx.graph(..., pinned=True)).
+    close() frees it; the arrays must not be used after."""
+
+    def __init__(self, hc, weighted):
+        self._hc = hc
+        n, m = hc.n, hc.m
+        self.offsets = np.ctypeslib.as_array(hc.offsets, shape=(n + 1,))
+        self.col = np.ctypeslib.as_array(hc.col, shape=(max(m, 1),))[:m]
+        self.weight = np.ctypeslib.as_array(hc.weight, shape=(max(m, 1),))[:m] if weighted else None
+        self.pinned = bool(hc.pinned)
+
+    def close(self):
+        if self._hc is not None:
+            self.offsets = self.col = self.weight = None
+            lib().ptg_host_csr_free(ctypes.byref(self._hc))
+            self._hc = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def gen_rmat_host(scale, edge_factor=16, a=0.57, b=0.19, c=0.19, seed=1, symmetric=True, wmin=0, wmax=0,
+                  threads=0, pinned=True):
+    """gen_rmat into library-owned (pinned) memory, returned as a HostGraph."""
+    hc = HostCsr()
+    _check(lib().ptg_gen_rmat(scale, edge_factor, a, b, c, seed, 1 if symmetric else 0, wmin, wmax,
+                              threads, 1 if pinned else 0, ctypes.byref(hc)))
+    return HostGraph(hc, wmax > 0)
+
+
 PTG_FILE_BCSR, PTG_FILE_BWCSR, PTG_FILE_JAVA, PTG_FILE_BCSR64 = 0, 1, 2, 3
 
 
