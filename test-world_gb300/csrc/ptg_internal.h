@@ -125,7 +125,8 @@ struct TravCtl {
     unsigned int level_val;       // BFS: value of current frontier vertices
     unsigned int error;           // nonzero: a kernel detected a bad index
     unsigned int bu_next;         // bottom-up BFS chunk counter (zero before each round)
-    unsigned int pad[3];
+    unsigned int bu_found;        // vertices a bottom-up round reached (its next frontier)
+    unsigned int pad[2];
 };
 
 // --------------------------------------------------------------------------

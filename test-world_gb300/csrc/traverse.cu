@@ -391,6 +391,10 @@ __global__ void __launch_bounds__(kBlock, 8) k_bottom_up(uint64_t n, const OffT 
     const unsigned lane = lane_id(), wid = threadIdx.x >> 5;
     const uint64_t words = (n + 31) / 32;
     const uint64_t chunks = (words + kBuWords - 1) / kBuWords;
+    // the next frontier's size (popcounts of the words written) and edge
+    // count, so the next push/pull choice needs no compaction pass
+    uint32_t found_cnt = 0;
+    unsigned long long found_deg = 0;
     while (true) {
         // warps take chunks from a shared counter: chunk costs vary a lot
         uint64_t chunk = 0;
@@ -445,9 +449,9 @@ __global__ void __launch_bounds__(kBlock, 8) k_bottom_up(uint64_t n, const OffT 
             for (int h = 0; h < 2; h++) {
                 if (h == 1 && !has2) break;
                 const uint32_t v = h ? v1 : v0;
-                const OffT e = h ? e1 : e0;
+                const OffT b = h ? b1 : b0, e = h ? e1 : e0;
                 bool found = f[h];
-                for (OffT k = (h ? b1 : b0) + 4; k < e && !found; k += 4) {
+                for (OffT k = b + 4; k < e && !found; k += 4) {
                     uint32_t c0 = col[k];
                     uint32_t c1 = k + 1 < e ? col[k + 1] : c0;
                     uint32_t c2 = k + 2 < e ? col[k + 2] : c0;
@@ -458,6 +462,7 @@ __global__ void __launch_bounds__(kBlock, 8) k_bottom_up(uint64_t n, const OffT 
                 if (found) {
                     atomicOr(&s_found[wid][(v >> 5) - (uint32_t)(cw0)], 1u << (v & 31u));
                     t.value[value_slot(t, v)] = newval;
+                    found_deg += (unsigned long long)(e - b);
                 }
             }
         }
@@ -466,8 +471,18 @@ __global__ void __launch_bounds__(kBlock, 8) k_bottom_up(uint64_t n, const OffT 
             uint32_t f = s_found[wid][lane];
             t.bm_next[wd] = f;
             if (f) t.vis[wd] = visw | f;
+            found_cnt += __popc(f);
         }
         __syncwarp();
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        found_cnt += __shfl_xor_sync(0xffffffffu, found_cnt, o);
+        found_deg += __shfl_xor_sync(0xffffffffu, found_deg, o);
+    }
+    if (lane == 0 && found_cnt) {
+        atomicAdd(&t.ctl->bu_found, found_cnt);
+        atomicAdd(&t.ctl->next_E, found_deg);
     }
 }
 
@@ -833,32 +848,32 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         unsigned long long *bsum = ws.bsum.as<unsigned long long>();
         OffT *sc = ws.scan.as<OffT>(), *rs = ws.rowstart.as<OffT>();
 
-        // direction decision needs the frontier's edge count first
-        bool small = F <= kSmallFrontier;
-        if (small) {
-            launch(ctx, "k_scan_small", k_scan_small<OffT>, 1, kBlock, 0, st, q_cur, d_ctl, off, clip, sc, rs);
-        } else {
-            launch(ctx, "k_scan_reduce", k_scan_reduce<OffT>, scan_blocks, kBlock, 0, st, q_cur, d_ctl, off,
-                   clip, bsum);
-            launch(ctx, "k_scan_bsums", k_scan_bsums, 1, kBlock, 0, st, bsum, scan_blocks, d_ctl);
-        }
         uint64_t E = 0;
         if (allow_bu) {
-            // the frontier's edge count came with its size (k_compact), so
-            // the push/pull choice needs no round trip of its own
+            // the frontier's edge count came with its size (k_compact, or the
+            // pull round that found it), so the push/pull choice needs no
+            // round trip of its own
             E = next_E;
             if (!bottom_up && (double)E > (double)m_unvisited / alpha) bottom_up = true;
             else if (bottom_up && (double)F < (double)n / beta) bottom_up = false;
             m_unvisited = m_unvisited > E ? m_unvisited - E : 0;
         }
         if (bottom_up) {
+            // a pull round reads the frontier bitmap: no queue scan
             rr.bottom_up_rounds++;
             launch(ctx, "k_bottom_up", k_bottom_up<OffT>, grid_for((words + kBuWords - 1) / kBuWords, kBuWarps, sms * 8),
                    kBlock, 0, st, n, off, col, bm_cur, (const uint32_t *)g->d_nzbm.as<uint32_t>(), pt);
         } else {
-            if (!small)
+            const bool small = F <= kSmallFrontier;
+            if (small) {
+                launch(ctx, "k_scan_small", k_scan_small<OffT>, 1, kBlock, 0, st, q_cur, d_ctl, off, clip, sc, rs);
+            } else {
+                launch(ctx, "k_scan_reduce", k_scan_reduce<OffT>, scan_blocks, kBlock, 0, st, q_cur, d_ctl, off,
+                       clip, bsum);
+                launch(ctx, "k_scan_bsums", k_scan_bsums, 1, kBlock, 0, st, bsum, scan_blocks, d_ctl);
                 launch(ctx, "k_scan_write", k_scan_write<OffT>, scan_blocks, kBlock, 0, st, q_cur, d_ctl, off,
                        clip, bsum, sc, rs);
+            }
             const int ecap = sms * (int)tu.expand_ctas_per_sm;
             int eg = ecap;
             if (allow_bu) eg = grid_for(E, kTile, ecap);
@@ -967,12 +982,29 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
                 if (link_open) PTG_CUDA_TRY(cudaEventRecord(g->link_ev[1], cs));
             }
         }
-        // next frontier: queue from the bitmap
-        launch(ctx, "k_compact", k_compact<OffT>, compact_grid, kBlock, 0, st, (const uint32_t *)bm_nxt, words, q_nxt,
-               d_ctl, vis, use_far ? ws.farbm.as<uint32_t>() : (uint32_t *)nullptr,
-               allow_bu ? off : (const OffT *)nullptr);
-        PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
-        PTG_CUDA_TRY(cudaStreamSynchronize(st));
+        // next frontier: queue from the bitmap.  A pull round counted what it
+        // found; when the next round pulls too (it stays pull unless the
+        // frontier is below n / beta) nothing reads a queue, so none is built.
+        bool need_queue = true;
+        if (bottom_up) {
+            PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
+            PTG_CUDA_TRY(cudaStreamSynchronize(st));
+            const uint64_t found = h_ctl->bu_found;
+            need_queue = found > 0 && (double)found < (double)n / beta;
+            if (!need_queue) h_ctl->next_tail = (uint32_t)found;  // F of the next (pull) round
+        }
+        if (need_queue) {
+            if (bottom_up) {  // k_compact counts the frontier and its edges again
+                TravCtl rst = *h_ctl;
+                rst.next_E = 0;
+                PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &rst, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
+            }
+            launch(ctx, "k_compact", k_compact<OffT>, compact_grid, kBlock, 0, st, (const uint32_t *)bm_nxt, words,
+                   q_nxt, d_ctl, vis, use_far ? ws.farbm.as<uint32_t>() : (uint32_t *)nullptr,
+                   allow_bu ? off : (const OffT *)nullptr);
+            PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
+            PTG_CUDA_TRY(cudaStreamSynchronize(st));
+        }
         PTG_REQUIRE(h_ctl->error == 0, PTG_ERR_CUDA, "frontier overflow in relax");
         if (link_open) {
             // the level's copies, first start to last end (the compute stream
@@ -990,6 +1022,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         upd.next_tail = 0;
         upd.next_E = 0;
         upd.bu_next = 0;
+        upd.bu_found = 0;
         level_val++;
         upd.level_val = level_val;
         PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &upd, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
