@@ -127,6 +127,7 @@ struct TravCtl {
     unsigned int bu_next;         // bottom-up BFS chunk counter (zero before each round)
     unsigned int bu_found;        // vertices a bottom-up round reached (its next frontier)
     unsigned int pad[2];
+    unsigned long long frontier_E;  // unclipped edges of the current frontier (k_level_advance)
 };
 
 // --------------------------------------------------------------------------

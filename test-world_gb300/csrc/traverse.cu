@@ -39,6 +39,7 @@
 //    active adjacency into a unified-memory buffer the GPU page-faults on,
 //    main.cu:1126-1156, 1336-1378).
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "frontier.cuh"
@@ -155,10 +156,14 @@ __device__ __forceinline__ uint32_t warp_bit_vertex(uint32_t word, uint32_t pre,
     return (uint32_t)((wd0 + lo) * 32 + __fns(w, 0, (int)(r - ex) + 1));
 }
 
+// After a pull round (skip_at below ~0) the kernel does nothing when the
+// round found skip_at vertices or more: the next round pulls too and reads
+// only the bitmap.
 template <class OffT>
 __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t *bm, uint64_t words, uint32_t *q,
                                                     TravCtl *ctl, uint32_t *vis, uint32_t *far_bm,
-                                                    const OffT *off) {
+                                                    const OffT *off, unsigned long long skip_at) {
+    if (ctl->bu_found >= skip_at) return;  // the same value in every thread
     unsigned long long degsum = 0;
     constexpr int kWarps = kBlock / 32;
     __shared__ uint32_t s_warp[kWarps];
@@ -223,6 +228,23 @@ __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t *bm, uint64_t
         degsum = block_reduce_sum(degsum);
         if (threadIdx.x == 0 && degsum) atomicAdd(&ctl->next_E, degsum);
     }
+}
+
+// End of a level, on the device (so the host only reads the control block):
+// the next frontier's size and unclipped edge count become the current
+// ones, the per-level counters restart and the level value advances.  A
+// pull round whose finds were not compacted (skip_at or more of them) gives
+// its own count as the frontier size.
+__global__ void k_level_advance(TravCtl *ctl, unsigned long long skip_at) {
+    uint32_t F = ctl->next_tail;
+    if (ctl->bu_found >= skip_at) F = ctl->bu_found;
+    ctl->F = F;
+    ctl->frontier_E = ctl->next_E;
+    ctl->next_tail = 0;
+    ctl->next_E = 0;
+    ctl->bu_next = 0;
+    ctl->bu_found = 0;
+    ctl->level_val += 1u;
 }
 
 // Load-balanced top-down expansion of the frontier's (resident) edges.
@@ -790,7 +812,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
     uint64_t next_E = 0;  // edges of the frontier (BFS direction choice); the seed level runs top-down
     bool far_nonempty = false;
     const int compact_grid = grid_for((words + 31) / 32, kBlock / 32, sms * 8);
-    uint32_t threshold = init.threshold, level_val = base;
+    uint32_t threshold = init.threshold;
     bool bottom_up = false;
     if (max_iters == 0) max_iters = (uint32_t)std::min<uint64_t>(0xFFFFFFF0ull, 4 * n + 16);
     const double alpha = tu.bfs_alpha, beta = tu.bfs_beta;
@@ -827,7 +849,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
                    (const TravCtl *)d_ctl);
             launch(ctx, "k_compact", k_compact<OffT>, compact_grid, kBlock, 0, st,
                    (const uint32_t *)ws.bm[cur].as<uint32_t>(), words, ws.q[cur].as<uint32_t>(), d_ctl,
-                   (uint32_t *)nullptr, (uint32_t *)nullptr, (const OffT *)nullptr);
+                   (uint32_t *)nullptr, (uint32_t *)nullptr, (const OffT *)nullptr, ~0ull);
             PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
             PTG_CUDA_TRY(cudaStreamSynchronize(st));
             F = h_ctl->next_tail;
@@ -983,28 +1005,20 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
             }
         }
         // next frontier: queue from the bitmap.  A pull round counted what it
-        // found; when the next round pulls too (it stays pull unless the
-        // frontier is below n / beta) nothing reads a queue, so none is built.
-        bool need_queue = true;
-        if (bottom_up) {
-            PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
-            PTG_CUDA_TRY(cudaStreamSynchronize(st));
-            const uint64_t found = h_ctl->bu_found;
-            need_queue = found > 0 && (double)found < (double)n / beta;
-            if (!need_queue) h_ctl->next_tail = (uint32_t)found;  // F of the next (pull) round
-        }
-        if (need_queue) {
-            if (bottom_up) {  // k_compact counts the frontier and its edges again
-                TravCtl rst = *h_ctl;
-                rst.next_E = 0;
-                PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &rst, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
-            }
-            launch(ctx, "k_compact", k_compact<OffT>, compact_grid, kBlock, 0, st, (const uint32_t *)bm_nxt, words,
-                   q_nxt, d_ctl, vis, use_far ? ws.farbm.as<uint32_t>() : (uint32_t *)nullptr,
-                   allow_bu ? off : (const OffT *)nullptr);
-            PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
-            PTG_CUDA_TRY(cudaStreamSynchronize(st));
-        }
+        // found (and folded it into the visited bitmap); when the next round
+        // pulls too (it stays pull unless the frontier is below n / beta)
+        // nothing reads a queue, and the compaction skips itself on the
+        // device.  Then the control block advances on the device, and the
+        // host reads it once.
+        const unsigned long long skip_at =
+            bottom_up ? (unsigned long long)std::ceil((double)n / beta) : ~0ull;
+        launch(ctx, "k_compact", k_compact<OffT>, compact_grid, kBlock, 0, st, (const uint32_t *)bm_nxt, words, q_nxt,
+               d_ctl, bottom_up ? (uint32_t *)nullptr : vis,
+               use_far ? ws.farbm.as<uint32_t>() : (uint32_t *)nullptr,
+               allow_bu && !bottom_up ? off : (const OffT *)nullptr, skip_at);
+        launch(ctx, "k_level_advance", k_level_advance, 1, 1, 0, st, d_ctl, skip_at);
+        PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
+        PTG_CUDA_TRY(cudaStreamSynchronize(st));
         PTG_REQUIRE(h_ctl->error == 0, PTG_ERR_CUDA, "frontier overflow in relax");
         if (link_open) {
             // the level's copies, first start to last end (the compute stream
@@ -1014,18 +1028,9 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
             rr.link_ms += lms;
             link_open = false;
         }
-        F = h_ctl->next_tail;
-        next_E = h_ctl->next_E;
+        F = h_ctl->F;
+        next_E = h_ctl->frontier_E;
         if (use_far) far_nonempty = true;
-        TravCtl upd = *h_ctl;
-        upd.F = (uint32_t)F;
-        upd.next_tail = 0;
-        upd.next_E = 0;
-        upd.bu_next = 0;
-        upd.bu_found = 0;
-        level_val++;
-        upd.level_val = level_val;
-        PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &upd, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
         cur ^= 1;
     }
     PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
