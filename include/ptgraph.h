@@ -225,7 +225,8 @@ typedef struct ptg_tuning {
     float bfs_beta;              /* ... and back to push when the frontier holds fewer
                                     than n / bfs_beta vertices (default 18)              */
     float sssp_delta_scale;      /* default SSSP bucket width = this x the mean edge
-                                    weight (default 2; 0: label-correcting rounds)       */
+                                    weight on graphs of 2^29+ edges, up to 4x wider on
+                                    smaller ones (default 0.75; 0: label-correcting)     */
     uint32_t expand_ctas_per_sm; /* push relax (k_expand) CTAs per SM, 1..32 (default 4) */
     uint32_t pr_ctas_per_sm;     /* PageRank SpMV CTAs per SM, 1..32 (default 8)         */
     uint32_t pr_mid;             /* PageRank rows of 5..pr_mid edges run 8 lanes per

@@ -274,7 +274,7 @@ void ptg_tuning_defaults(ptg_tuning *t) {
     t->version = PTG_TUNING_VERSION;
     t->bfs_alpha = 15.f;
     t->bfs_beta = 18.f;
-    t->sssp_delta_scale = 2.0f;
+    t->sssp_delta_scale = 0.75f;
     t->expand_ctas_per_sm = 4;
     t->pr_ctas_per_sm = 8;
     t->pr_mid = 256;

@@ -375,6 +375,18 @@ __device__ __forceinline__ void ms_shfl_add(ff (&acc)[K], int o, int width) {
     for (int s = 0; s < K; s++) acc[s] = ff_add(acc[s], ff_shfl_xor(acc[s], o, width));
 }
 
+// Neighbours in flight per lane in the batched passes, and their CTAs per
+// SM: the K-wide sums and loads take registers, and at RMAT-26 (2.1 GB of
+// 8-wide values, gathered from DRAM) two loads per lane at 4 CTAs of 256
+// per SM beat four loads at 3 CTAs (498 vs 570 ms per 8-source pass).  The
+// per-lane order of additions does not depend on it.
+constexpr int kPrkBatch = 2;
+constexpr int kPrkMinBlocks = 4;
+
+// A vertex without edges that is none of the pass's sources keeps 0 in both
+// value buffers (both start zeroed), so it is skipped: on RMAT graphs about
+// half the vertices are isolated, and writing their K values each iteration
+// was a third of this kernel's time.
 template <class OffT, int K>
 __global__ void __launch_bounds__(kBlock) k_prk_small(MsArgs a) {
     const OffT *off = reinterpret_cast<const OffT *>(a.off);
@@ -382,6 +394,12 @@ __global__ void __launch_bounds__(kBlock) k_prk_small(MsArgs a) {
         OffT b = off[v], e = off[v + 1];
         OffT deg = e - b;
         if ((uint64_t)deg > kPrSmall) continue;
+        if (deg == 0) {
+            bool is_src = false;
+#pragma unroll
+            for (int s = 0; s < K; s++) is_src |= v == a.src[s];
+            if (!is_src) continue;
+        }
         ff acc[K];
 #pragma unroll
         for (int s = 0; s < K; s++) acc[s] = ff{0.f, 0.f};
@@ -391,7 +409,7 @@ __global__ void __launch_bounds__(kBlock) k_prk_small(MsArgs a) {
 }
 
 template <class OffT, int K>
-__global__ void __launch_bounds__(kBlock) k_prk_mid(MsArgs a, PrBins bins) {
+__global__ void __launch_bounds__(kBlock, kPrkMinBlocks) k_prk_mid(MsArgs a, PrBins bins) {
     const OffT *off = reinterpret_cast<const OffT *>(a.off);
     const unsigned sub = threadIdx.x & 7u;
     const uint64_t groups = (uint64_t)gridDim.x * blockDim.x / 8;
@@ -403,7 +421,7 @@ __global__ void __launch_bounds__(kBlock) k_prk_mid(MsArgs a, PrBins bins) {
         ff acc[K];
 #pragma unroll
         for (int s = 0; s < K; s++) acc[s] = ff{0.f, 0.f};
-        ms_run<K, 4>(a, b + sub, e, 8, acc);
+        ms_run<K, kPrkBatch>(a, b + sub, e, 8, acc);
 #pragma unroll
         for (int o = 4; o > 0; o >>= 1) ms_shfl_add<K>(acc, o, 8);
         if (valid && sub == 0) ms_finalize<OffT, K>(a, v, e - b, acc);
@@ -411,7 +429,7 @@ __global__ void __launch_bounds__(kBlock) k_prk_mid(MsArgs a, PrBins bins) {
 }
 
 template <class OffT, int K>
-__global__ void __launch_bounds__(kBlock) k_prk_big(MsArgs a, PrBins bins) {
+__global__ void __launch_bounds__(kBlock, kPrkMinBlocks) k_prk_big(MsArgs a, PrBins bins) {
     const OffT *off = reinterpret_cast<const OffT *>(a.off);
     const unsigned lane = lane_id();
     const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
@@ -421,7 +439,7 @@ __global__ void __launch_bounds__(kBlock) k_prk_big(MsArgs a, PrBins bins) {
         ff acc[K];
 #pragma unroll
         for (int s = 0; s < K; s++) acc[s] = ff{0.f, 0.f};
-        ms_run<K, 4>(a, b + lane, e, 32, acc);
+        ms_run<K, kPrkBatch>(a, b + lane, e, 32, acc);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) ms_shfl_add<K>(acc, o, 32);
         if (lane == 0) ms_finalize<OffT, K>(a, v, e - b, acc);
@@ -429,7 +447,7 @@ __global__ void __launch_bounds__(kBlock) k_prk_big(MsArgs a, PrBins bins) {
 }
 
 template <class OffT, int K>
-__global__ void __launch_bounds__(kBlock) k_prk_chunks(MsArgs a, PrBins bins) {
+__global__ void __launch_bounds__(kBlock, kPrkMinBlocks) k_prk_chunks(MsArgs a, PrBins bins) {
     const OffT *off = reinterpret_cast<const OffT *>(a.off);
     const unsigned lane = lane_id();
     const uint64_t warps = (uint64_t)gridDim.x * blockDim.x / 32;
@@ -441,7 +459,7 @@ __global__ void __launch_bounds__(kBlock) k_prk_chunks(MsArgs a, PrBins bins) {
         ff acc[K];
 #pragma unroll
         for (int s = 0; s < K; s++) acc[s] = ff{0.f, 0.f};
-        ms_run<K, 4>(a, b + lane, e, 32, acc);
+        ms_run<K, kPrkBatch>(a, b + lane, e, 32, acc);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) ms_shfl_add<K>(acc, o, 32);
         if (lane == 0)
@@ -691,7 +709,7 @@ void ppr_multi_impl(ptg_graph *g, const uint32_t *h_srcs, uint32_t k, float *d_r
     for (int s = 0; s < K; s++) lanes[s] = (uint32_t)s < k ? h_srcs[s] : 0xFFFFFFFFu;
     PTG_CUDA_TRY(cudaMemcpyAsync(d_src, lanes, sizeof(lanes), cudaMemcpyHostToDevice, st));
     map_sources_dev(g, d_src, K);
-    PTG_CUDA_TRY(cudaMemsetAsync(c[0], 0, n * K * 4, st));
+    PTG_CUDA_TRY(cudaMemsetAsync(c[0], 0, 2 * n * K * 4, st));  // both buffers (isolated vertices stay 0)
     const OffT *off = g->d_off.as<OffT>();
     launch(ctx, "k_prk_init", k_prk_init<OffT, K>, 1, 32, 0, st, off, (const uint32_t *)d_src, c[0], dang);
     PrBins bins;

@@ -778,10 +778,16 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         init.level_val = base;
         if (use_far) {
             if (delta == 0) {
-                // default bucket width: a tuned fraction (half) of the mean edge
-                // weight, measured once per graph
+                // default bucket width: the tuned multiple of the mean edge
+                // weight (measured once per graph) for graphs of 2^29+ edges,
+                // widened up to 4x as the graph shrinks.  Each bucket costs a
+                // few rounds of fixed cost (launches, a host round trip),
+                // while the re-relaxations narrow buckets save grow with m:
+                // RMAT-24 (5.2e8 edges) is fastest at 0.75x the mean weight,
+                // RMAT-20 and -22 at 3x.
                 measure_mean_weight(g);
-                double scale = tu.sssp_delta_scale;
+                const double widen = std::min(4.0, std::max(1.0, 536870912.0 / (double)std::max<uint64_t>(1, g->m)));
+                const double scale = tu.sssp_delta_scale * widen;
                 delta = (uint32_t)std::min(1e9, std::max(1.0, g->mean_weight > 0 ? g->mean_weight * scale : 64.0 * scale));
             }
             init.threshold = base + delta;

@@ -50,7 +50,7 @@ CANDIDATES = {
     "bfs_alpha": [6.0, 10.0, 15.0, 22.0, 32.0],
     "bfs_beta": [8.0, 12.0, 18.0, 24.0, 36.0],
     "expand_ctas_per_sm": [2, 3, 4, 6, 8, 12, 16],
-    "sssp_delta_scale": [0.25, 0.5, 1.0, 2.0, 4.0, 8.0],
+    "sssp_delta_scale": [0.25, 0.5, 0.75, 1.0, 2.0, 4.0],
     "ms_pull_small": [8, 16, 32, 64, 128],
     "ms_pull_chunk": [256, 512, 1024, 2048, 4096],
     "vertex_order": [0, 1],
