@@ -952,29 +952,58 @@ def e2e_measure(ctx, off32, col, w, sources, args, deg, step_edges, n, m):
             "cc": torch.empty(n, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32),
             "pr": torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()}
 
-    def step():
+    # the link's rate from these very buffers (the floor under the upload)
+    probe = torch.empty(col.size, dtype=torch.int32, device="cuda")
+    src = torch.from_numpy(ph["col"].view(np.int32))
+    link = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        probe.copy_(src, non_blocking=True)
+        torch.cuda.synchronize()
+        link.append(col.nbytes / (time.perf_counter() - t0) / 1e9)
+    del probe
+    phases = dict.fromkeys(("create", "bfs", "sssp", "cc", "pagerank", "destroy"), 0.0)
+
+    def step(acc):
+        # every call returns with its result in host memory (the API is
+        # synchronous), so the host clock between calls splits the step
+        t = [time.perf_counter()]
+
+        def mark(name):
+            t.append(time.perf_counter())
+            if acc is not None:
+                acc[name] += t[-1] - t[-2]
         G = ctx.graph(ph["off"], ph["col"], ph["w"], symmetric=True, pinned=True)
+        mark("create")
         for s in sources:
             G.bfs(int(s), out=outs["bfs"])
+        mark("bfs")
         for s in sources[:args.sssp_sources]:
             G.sssp(int(s), out=outs["sssp"])
+        mark("sssp")
         G.cc(out=outs["cc"])
+        mark("cc")
         G.pagerank(out=outs["pr"])
+        mark("pagerank")
         G.close()
+        mark("destroy")
 
     for _ in range(min(2, args.warmup)):
-        step()
+        step(None)
     torch.cuda.synchronize()
     k = max(1, min(5, args.steps))
     t0 = time.perf_counter()
     for _ in range(k):
-        step()
+        step(phases)
     torch.cuda.synchronize()
     dt = (time.perf_counter() - t0) / k
     h2d = off32.nbytes + col.nbytes + w.nbytes
     d2h = 4 * n * (len(sources) + args.sssp_sources + 2)
     return {"value": step_edges / dt / 1e9, "unit": "GTEPS", "h2d_bytes_per_step": int(h2d),
             "d2h_bytes_per_step": int(d2h), "ms_per_step": dt * 1e3,
+            "phases_ms": {p: round(v / k * 1e3, 2) for p, v in phases.items()},
+            "h2d_gbs_of_inputs": round(max(link), 1),
             "path": "ptg_graph_create from pinned host CSR + ptg_bfs/sssp/cc/pagerank into host buffers"}
 
 

@@ -189,11 +189,20 @@ typedef struct ptg_pr_opts {
 typedef struct ptg_ctx ptg_ctx;
 typedef struct ptg_graph ptg_graph;
 
+/* Device memory: blocks of 1 MiB and more that the engine frees (a destroyed
+ * graph's arrays, staging pieces) are kept per device for the next request
+ * of about their size, up to a quarter of the device's memory, while any
+ * context on that device is open; they count as free in free_bytes and in
+ * the partition planner, and are released when a cudaMalloc of the engine
+ * fails, when the device's last context is destroyed, or by
+ * ptg_ctx_release_cache.  A free waits for the device as cudaFree does. */
 ptg_status ptg_ctx_create(int device, ptg_ctx **out);
 void ptg_ctx_destroy(ptg_ctx *ctx);
+ptg_status ptg_ctx_release_cache(ptg_ctx *ctx);
 /* Message of the last failure on this context (thread-safe per context). */
 const char *ptg_ctx_last_error(const ptg_ctx *ctx);
-/* Device properties the engine sized itself for. */
+/* Device properties the engine sized itself for (free_bytes: cudaMemGetInfo's
+ * free memory plus the engine's cached blocks on the device). */
 ptg_status ptg_ctx_device_info(const ptg_ctx *ctx, int *sm_count, uint64_t *hbm_bytes,
                                uint64_t *free_bytes);
 

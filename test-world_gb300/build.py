@@ -14,7 +14,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libptgraph.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "traverse.cu", "cc.cu", "pagerank.cu", "batch.cu", "msbfs.cu", "serve.cu", "gen.cpp",
+SOURCES = ["devmem.cpp", "api.cu", "traverse.cu", "cc.cu", "pagerank.cu", "batch.cu", "msbfs.cu", "serve.cu", "gen.cpp",
            "noalloc.cu", "pprbatch.cu", "io.cpp", "relabel.cu", "compat_cxx.cpp"]
 
 

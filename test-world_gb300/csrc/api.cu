@@ -124,17 +124,28 @@ std::vector<uint64_t> host_offsets(const ptg_csr *c) {
     return o;
 }
 
-// The caller's offsets read in place: u32 or u64, n or n + 1 entries (the
-// reference's n-entry form ends at m).
-struct HostOffsets {
-    const void *p;
-    bool u64, sentinel;
-    uint64_t n, m;
-    uint64_t operator[](uint64_t i) const {
-        if (i == n && !sentinel) return m;
-        return u64 ? static_cast<const uint64_t *>(p)[i] : static_cast<const uint32_t *>(p)[i];
+// Caller rows cut into pieces of at most `per` edges (a longer row is a
+// piece of its own): rows [cut_v[i], cut_v[i+1]) hold edges
+// [cut_e[i], cut_e[i+1]).  The offsets must be non-decreasing.
+void edge_pieces(const HostOffsets &off, uint64_t n, uint64_t per, std::vector<uint64_t> &cut_v,
+                 std::vector<uint64_t> &cut_e) {
+    per = std::max<uint64_t>(per, 1);
+    cut_v.assign(1, 0);
+    cut_e.assign(1, off[0]);
+    for (uint64_t v = 0; v < n;) {
+        const uint64_t lim = off[v] + per;
+        uint64_t lo = v + 1, hi = n;  // the last w in [v+1, n] with off[w] <= lim, at least v+1
+        if (off[lo] <= lim)
+            while (lo < hi) {
+                uint64_t mid = lo + (hi - lo + 1) / 2;
+                if (off[mid] <= lim) lo = mid;
+                else hi = mid - 1;
+            }
+        v = lo;
+        cut_v.push_back(v);
+        cut_e.push_back(off[v]);
     }
-};
+}
 
 void plan(uint64_t n, uint64_t m, const HostOffsets &off, uint64_t bpe, const ptg_partition_config *cfg_in,
           uint64_t device_free, uint64_t &P, uint64_t &R, uint64_t &PE, std::vector<uint64_t> *first) {
@@ -343,6 +354,8 @@ ptg_status ptg_ctx_create(int device, ptg_ctx **out) {
         PTG_CUDA_TRY(cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking));
         PTG_CUDA_TRY(cudaEventCreate(&ctx->ev0));
         PTG_CUDA_TRY(cudaEventCreate(&ctx->ev1));
+        dev_context_opened(device, ctx->hbm_bytes);
+        ctx->holds_cache = true;
     });
     if (s != PTG_OK) {
         ptg_ctx_destroy(ctx);
@@ -361,7 +374,17 @@ void ptg_ctx_destroy(ptg_ctx *ctx) {
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
-    delete ctx;
+    const int dev = ctx->device;
+    const bool held = ctx->holds_cache;
+    delete ctx;  // its buffers go to the device's block cache first
+    if (held) dev_context_closed(dev);
+}
+
+ptg_status ptg_ctx_release_cache(ptg_ctx *ctx) {
+    if (!ctx) return PTG_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    dev_cache_release(ctx->device);
+    return PTG_OK;
 }
 
 const char *ptg_ctx_last_error(const ptg_ctx *ctx) { return ctx ? ctx->last_error.c_str() : ""; }
@@ -399,7 +422,7 @@ ptg_status ptg_ctx_device_info(const ptg_ctx *ctx, int *sm_count, uint64_t *hbm_
     if (free_bytes) {
         size_t f = 0, t = 0;
         cudaSetDevice(ctx->device);
-        if (cudaMemGetInfo(&f, &t) != cudaSuccess) return PTG_ERR_CUDA;
+        if (device_free_bytes(ctx->device, &f, &t) != cudaSuccess) return PTG_ERR_CUDA;
         *free_bytes = f;
     }
     return PTG_OK;
@@ -456,7 +479,7 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
         if (cfg.n_staging_buffers > 3) cfg.n_staging_buffers = 3;
         uint64_t bpe = g->weighted ? 8 : 4;
         size_t dfree = 0, dtot = 0;
-        PTG_CUDA_TRY(cudaMemGetInfo(&dfree, &dtot));
+        PTG_CUDA_TRY(device_free_bytes(ctx->device, &dfree, &dtot));
         // keep room for the traversal workspace (~40 bytes per vertex, the
         // reference's own reserve is 10 * 4 * n, main.cu:1193)
         uint64_t reserve = 48ull * g->n + (512ull << 20);
@@ -507,54 +530,84 @@ ptg_status ptg_graph_create(ptg_ctx *ctx, const ptg_csr *csr, const ptg_partitio
 
         // resident edges (SoA in HBM)
         uint64_t RE = g->resident_edges;
-        g->d_col.ensure(std::max<uint64_t>(RE, 1) * 4);
-        if (g->weighted) g->d_w.ensure(std::max<uint64_t>(RE, 1) * 4);
-        if (RE) {
-            if (csr->col) {
-                PTG_CUDA_TRY(cudaMemcpyAsync(g->d_col.p, csr->col, RE * 4, cudaMemcpyHostToDevice, st));
-                if (csr->weight)
-                    PTG_CUDA_TRY(cudaMemcpyAsync(g->d_w.p, csr->weight, RE * 4, cudaMemcpyHostToDevice, st));
-            } else {
-                // reference AoS records: stage through HBM in chunks and split
-                DevBuf tmp;
-                uint64_t chunk = std::min<uint64_t>(RE, 1ull << 26);
-                tmp.ensure(chunk * 8);
-                for (uint64_t e = 0; e < RE; e += chunk) {
-                    uint64_t c = std::min<uint64_t>(chunk, RE - e);
-                    PTG_CUDA_TRY(cudaMemcpyAsync(tmp.p, csr->edges_aos + e, c * 8, cudaMemcpyHostToDevice, st));
-                    launch(ctx, "k_aos_to_soa", k_aos_to_soa, grid_for(c, kBlock, ctx->sm_count * 8), kBlock, 0,
-                           st, tmp.as<ptg_edge_w>(), c, g->d_col.as<uint32_t>() + e, g->d_w.as<uint32_t>() + e);
-                    PTG_CUDA_TRY(cudaStreamSynchronize(st));
+        DevBuf bad;
+        bad.ensure(4);
+        bool built = false;
+        if (RE == g->m && g->m && csr->col) {
+            // A graph that will be regrouped is built while its edges cross
+            // the link: the offsets are checked first, the regrouped order
+            // follows from them alone, and the edges arrive in pieces of
+            // about 8 partitions (256 MiB by default) that are regrouped as
+            // they land.
+            PTG_CUDA_TRY(cudaMemsetAsync(bad.p, 0, 4, st));
+            if (g->off64)
+                launch(ctx, "k_validate", k_validate<unsigned long long>, ctx->sm_count * 8, kBlock, 0, st,
+                       g->d_off.as<unsigned long long>(), g->n, g->m, (const uint32_t *)nullptr, (uint64_t)0,
+                       bad.as<unsigned>());
+            else
+                launch(ctx, "k_validate", k_validate<uint32_t>, ctx->sm_count * 8, kBlock, 0, st,
+                       g->d_off.as<uint32_t>(), g->n, g->m, (const uint32_t *)nullptr, (uint64_t)0,
+                       bad.as<unsigned>());
+            unsigned hb = 0;
+            PTG_CUDA_TRY(cudaMemcpyAsync(&hb, bad.p, 4, cudaMemcpyDeviceToHost, st));
+            PTG_CUDA_TRY(cudaStreamSynchronize(st));
+            PTG_REQUIRE(!(hb & 1), PTG_ERR_INVALID, "offsets are not non-decreasing within [0, m]");
+            std::vector<uint64_t> cut_v, cut_e;
+            edge_pieces(off, g->n, 8 * PE, cut_v, cut_e);
+            try {
+                built = relabel_graph_streamed(g, off, csr->col, csr->weight, cut_v, cut_e);
+            } catch (const Error &e) {
+                if (e.status != PTG_ERR_OOM) throw;
+                cudaGetLastError();
+            }
+        }
+        if (!built) {  // the edges as given, then regrouped on the device
+            g->d_col.ensure(std::max<uint64_t>(RE, 1) * 4);
+            if (g->weighted) g->d_w.ensure(std::max<uint64_t>(RE, 1) * 4);
+            if (RE) {
+                if (csr->col) {
+                    PTG_CUDA_TRY(cudaMemcpyAsync(g->d_col.p, csr->col, RE * 4, cudaMemcpyHostToDevice, st));
+                    if (csr->weight)
+                        PTG_CUDA_TRY(cudaMemcpyAsync(g->d_w.p, csr->weight, RE * 4, cudaMemcpyHostToDevice, st));
+                } else {
+                    // reference AoS records: stage through HBM in chunks and split
+                    DevBuf tmp;
+                    uint64_t chunk = std::min<uint64_t>(RE, 1ull << 26);
+                    tmp.ensure(chunk * 8);
+                    for (uint64_t e = 0; e < RE; e += chunk) {
+                        uint64_t c = std::min<uint64_t>(chunk, RE - e);
+                        PTG_CUDA_TRY(cudaMemcpyAsync(tmp.p, csr->edges_aos + e, c * 8, cudaMemcpyHostToDevice, st));
+                        launch(ctx, "k_aos_to_soa", k_aos_to_soa, grid_for(c, kBlock, ctx->sm_count * 8), kBlock, 0,
+                               st, tmp.as<ptg_edge_w>(), c, g->d_col.as<uint32_t>() + e, g->d_w.as<uint32_t>() + e);
+                        PTG_CUDA_TRY(cudaStreamSynchronize(st));
+                    }
                 }
+            }
+            // validate on the device
+            PTG_CUDA_TRY(cudaMemsetAsync(bad.p, 0, 4, st));
+            if (g->off64)
+                launch(ctx, "k_validate", k_validate<unsigned long long>, ctx->sm_count * 8, kBlock, 0, st,
+                       g->d_off.as<unsigned long long>(), g->n, g->m, g->d_col.as<uint32_t>(), RE, bad.as<unsigned>());
+            else
+                launch(ctx, "k_validate", k_validate<uint32_t>, ctx->sm_count * 8, kBlock, 0, st,
+                       g->d_off.as<uint32_t>(), g->n, g->m, g->d_col.as<uint32_t>(), RE, bad.as<unsigned>());
+            unsigned hbad = 0;
+            PTG_CUDA_TRY(cudaMemcpyAsync(&hbad, bad.p, 4, cudaMemcpyDeviceToHost, st));
+            PTG_CUDA_TRY(cudaStreamSynchronize(st));
+            PTG_REQUIRE(!(hbad & 1), PTG_ERR_INVALID, "offsets are not non-decreasing within [0, m]");
+            PTG_REQUIRE(!(hbad & 2), PTG_ERR_INVALID, "an edge target is >= n");
+            // degree-grouped vertex order, when the tuning asks for it.  The
+            // rebuild holds two copies of the edges for a moment; if that memory
+            // is not there the graph stays in the caller's order (nothing was
+            // swapped yet: the rebuild's buffers are released on the way out).
+            try {
+                relabel_graph(g);
+            } catch (const Error &e) {
+                if (e.status != PTG_ERR_OOM) throw;
+                cudaGetLastError();
             }
         }
         g->device_bytes += RE * bpe;
-
-        // validate on the device
-        DevBuf bad;
-        bad.ensure(4);
-        PTG_CUDA_TRY(cudaMemsetAsync(bad.p, 0, 4, st));
-        if (g->off64)
-            launch(ctx, "k_validate", k_validate<unsigned long long>, ctx->sm_count * 8, kBlock, 0, st,
-                   g->d_off.as<unsigned long long>(), g->n, g->m, g->d_col.as<uint32_t>(), RE, bad.as<unsigned>());
-        else
-            launch(ctx, "k_validate", k_validate<uint32_t>, ctx->sm_count * 8, kBlock, 0, st,
-                   g->d_off.as<uint32_t>(), g->n, g->m, g->d_col.as<uint32_t>(), RE, bad.as<unsigned>());
-        unsigned hbad = 0;
-        PTG_CUDA_TRY(cudaMemcpyAsync(&hbad, bad.p, 4, cudaMemcpyDeviceToHost, st));
-        PTG_CUDA_TRY(cudaStreamSynchronize(st));
-        PTG_REQUIRE(!(hbad & 1), PTG_ERR_INVALID, "offsets are not non-decreasing within [0, m]");
-        PTG_REQUIRE(!(hbad & 2), PTG_ERR_INVALID, "an edge target is >= n");
-        // degree-grouped vertex order, when the tuning asks for it.  The
-        // rebuild holds two copies of the edges for a moment; if that memory
-        // is not there the graph stays in the caller's order (nothing was
-        // swapped yet: the rebuild's buffers are released on the way out).
-        try {
-            relabel_graph(g);
-        } catch (const Error &e) {
-            if (e.status != PTG_ERR_OOM) throw;
-            cudaGetLastError();
-        }
 
         if (g->out_of_core) {
             // host side of the streamed partitions: pinned SoA arrays

@@ -554,6 +554,7 @@ inline void ms_next(ptg_ctx *ctx, Workspace &ws, uint64_t &F, uint64_t &Eact, ui
     E = h_ctl->E;
     std::swap(ws.q[0].p, ws.q[1].p);
     std::swap(ws.q[0].bytes, ws.q[1].bytes);
+    std::swap(ws.q[0].dev, ws.q[1].dev);
     TravCtl upd{};
     upd.F = (uint32_t)F;
     PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &upd, sizeof(TravCtl), cudaMemcpyHostToDevice, st));

@@ -56,24 +56,37 @@ struct Error {
 // --------------------------------------------------------------------------
 // device buffer (RAII)
 // --------------------------------------------------------------------------
+// Device blocks (devmem.cpp): blocks of 1 MiB and more are cached when freed
+// and reused for requests of about their size; bytes may be rounded up.
+void *dev_alloc(size_t &bytes, int dev);
+void dev_free(void *p, size_t bytes, int dev);
+size_t dev_cached_bytes(int dev);
+void dev_context_opened(int dev, size_t hbm_bytes);
+void dev_context_closed(int dev);
+void dev_cache_release(int dev);
+// cudaMemGetInfo of `dev` with the cached blocks counted as free
+cudaError_t device_free_bytes(int dev, size_t *free_bytes, size_t *total_bytes);
+
 struct DevBuf {
     void *p = nullptr;
     size_t bytes = 0;
+    int dev = 0;
     DevBuf() = default;
     DevBuf(const DevBuf &) = delete;
     DevBuf &operator=(const DevBuf &) = delete;
     ~DevBuf() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        if (p) dev_free(p, bytes, dev);
         p = nullptr;
         bytes = 0;
     }
-    // grow-only reallocation
+    // grow-only reallocation on the current device
     void ensure(size_t want) {
         if (want <= bytes && p) return;
         release();
         size_t b = want ? want : 16;
-        PTG_CUDA_TRY(cudaMalloc(&p, b));
+        PTG_CUDA_TRY(cudaGetDevice(&dev));
+        p = dev_alloc(b, dev);
         bytes = b;
     }
     template <class T>
@@ -223,6 +236,7 @@ struct ptg_ctx {
     uint64_t hbm_bytes = 0;
     cudaStream_t stream = nullptr;       // compute stream
     cudaStream_t copy_stream = nullptr;  // host->device partition stream
+    bool holds_cache = false;            // counted by the device block cache (devmem.cpp)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::mutex mu;                       // one query at a time per context
     std::string last_error;
@@ -333,10 +347,29 @@ int sm_count_of(ptg_ctx *ctx);
 // first use.
 void pr_prepare_graph(ptg_graph *g);
 
+// The caller's offsets read in place: u32 or u64, n or n + 1 entries (the
+// reference's n-entry form ends at m).
+struct HostOffsets {
+    const void *p;
+    bool u64, sentinel;
+    uint64_t n, m;
+    uint64_t operator[](uint64_t i) const {
+        if (i == n && !sentinel) return m;
+        return u64 ? static_cast<const uint64_t *>(p)[i] : static_cast<const uint32_t *>(p)[i];
+    }
+};
+
 // Vertex order (relabel.cu).  relabel_graph regroups a resident symmetric
 // graph's vertices by degree when the context's tuning asks for it (returns
 // whether it did); the helpers map sources in and results out.
 bool relabel_graph(ptg_graph *g);
+// The same while the caller's edges are uploaded: caller rows [cut_v[i],
+// cut_v[i+1]) with edges [cut_e[i], cut_e[i+1]) are copied and regrouped a
+// piece at a time.  Needs the offsets on the device (checked) and nothing
+// else; returns false, with the graph untouched, when the order is not
+// wanted or the memory is not there.  Edge targets >= n fail PTG_ERR_INVALID.
+bool relabel_graph_streamed(ptg_graph *g, const HostOffsets &host_off, const uint32_t *h_col, const uint32_t *h_w,
+                            const std::vector<uint64_t> &cut_v, const std::vector<uint64_t> &cut_e);
 void map_sources_dev(ptg_graph *g, uint32_t *d_ids, uint32_t k);
 uint32_t map_source_host(ptg_graph *g, uint32_t src);
 void unpermute_u32(ptg_graph *g, const uint32_t *tmp, uint32_t *out, uint32_t rows);

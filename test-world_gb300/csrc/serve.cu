@@ -119,6 +119,7 @@ ptg_graph *make_view(ptg_graph *g, ptg_ctx *lane) {
     auto alias = [](DevBuf &dst, const DevBuf &src) {
         dst.p = src.p;
         dst.bytes = src.bytes;
+        dst.dev = src.dev;
     };
     alias(v->d_off, g->d_off);
     alias(v->d_col, g->d_col);
@@ -510,7 +511,7 @@ ptg_status ptg_server_create(ptg_ctx *ctx, const ptg_server_config *cfg, ptg_ser
     }
     size_t dfree = 0, dtot = 0;
     cudaSetDevice(ctx->device);
-    if (cudaMemGetInfo(&dfree, &dtot) != cudaSuccess) {
+    if (device_free_bytes(ctx->device, &dfree, &dtot) != cudaSuccess) {
         cudaGetLastError();
         delete s;
         return PTG_ERR_CUDA;

@@ -174,6 +174,7 @@ _SIGS = {
                                            _u64p, _u64p, _u64p]),
     "ptg_ctx_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_vp)]),
     "ptg_ctx_destroy": (None, [_vp]),
+    "ptg_ctx_release_cache": (ctypes.c_int, [_vp]),
     "ptg_ctx_last_error": (ctypes.c_char_p, [_vp]),
     "ptg_ctx_device_info": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int), _u64p, _u64p]),
     "ptg_ctx_profile_enable": (ctypes.c_int, [_vp, ctypes.c_int]),
@@ -324,6 +325,10 @@ class Ctx:
         _check(lib().ptg_ctx_device_info(self.h, ctypes.byref(sms), ctypes.byref(hbm),
                                          ctypes.byref(free)), self.h)
         return {"sm_count": sms.value, "hbm_bytes": hbm.value, "free_bytes": free.value}
+
+    def release_cache(self):
+        """Return the engine's cached device blocks on this device to the driver."""
+        _check(lib().ptg_ctx_release_cache(self.h), self.h)
 
     def tuning(self):
         """The context's tuning knobs as a dict."""
