@@ -106,23 +106,45 @@ __global__ void __launch_bounds__(kBlock) k_scan_write(const uint32_t *q, const 
 // Small frontiers (most rounds): one CTA does the work of k_scan_reduce,
 // k_scan_bsums and k_scan_write in a single launch.
 constexpr uint32_t kSmallFrontier = 16384;
+// With tr, it also writes the tile rows of k_tile_rows: the entry whose
+// edges hold a tile's first edge writes that tile's row (a warp per such
+// entry), and tr[ntiles] = F - 1, as last_le gives them.
 template <class OffT>
 __global__ void __launch_bounds__(kBlock) k_scan_small(const uint32_t *q, TravCtl *ctl, const OffT *off,
-                                                       OffT clip, OffT *sc, OffT *rs) {
+                                                       OffT clip, OffT *sc, OffT *rs, uint32_t *tr) {
     uint64_t F = ctl->F;
     unsigned long long run = 0;
+    const unsigned lane = lane_id();
     for (uint64_t base = 0; base < F; base += kBlock * kScanItems) {
         const uint64_t i0 = base + threadIdx.x * kScanItems;
         OffT d[kScanItems], st[kScanItems];
         unsigned long long tot;
         unsigned long long ex = block_exclusive_scan(scan_items(q, off, clip, i0, F, d, st), tot);
+        unsigned long long t_lo[kScanItems], t_hi[kScanItems];
 #pragma unroll
         for (int k = 0; k < kScanItems; k++) {
+            const unsigned long long at = run + ex;
             if (i0 + k < F) {
-                sc[i0 + k] = (OffT)(run + ex);
+                sc[i0 + k] = (OffT)at;
                 rs[i0 + k] = st[k];
             }
+            t_lo[k] = (at + kTile - 1) / kTile;  // tiles whose first edge is in [at, at + d)
+            t_hi[k] = (at + (unsigned long long)d[k] + kTile - 1) / kTile;
             ex += (unsigned long long)d[k];
+        }
+        if (tr) {
+#pragma unroll
+            for (int k = 0; k < kScanItems; k++) {
+                unsigned has = __ballot_sync(0xffffffffu, i0 + k < F && t_hi[k] > t_lo[k]);
+                while (has) {
+                    const int src = __ffs(has) - 1;
+                    has &= has - 1;
+                    const unsigned long long a = __shfl_sync(0xffffffffu, t_lo[k], src);
+                    const unsigned long long b = __shfl_sync(0xffffffffu, t_hi[k], src);
+                    const uint32_t row = (uint32_t)__shfl_sync(0xffffffffu, i0 + k, src);
+                    for (unsigned long long t = a + lane; t < b; t += 32) tr[t] = row;
+                }
+            }
         }
         run += tot;
     }
@@ -130,6 +152,7 @@ __global__ void __launch_bounds__(kBlock) k_scan_small(const uint32_t *q, TravCt
         sc[F] = (OffT)run;
         ctl->E = run;
         ctl->edges_done += run;
+        if (tr) tr[(run + kTile - 1) / kTile] = (uint32_t)(F ? F - 1 : 0);
     }
 }
 

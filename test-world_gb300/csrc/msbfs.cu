@@ -483,16 +483,17 @@ void ms_scan(ptg_ctx *ctx, Workspace &ws, const OffT *off, uint64_t m, uint64_t 
     OffT *sc = ws.scan.as<OffT>(), *rs = ws.rowstart.as<OffT>();
     unsigned long long *bsum = ws.bsum.as<unsigned long long>();
     const uint32_t *q = ws.q[0].as<uint32_t>();
-    if (F <= kSmallFrontier) {
-        launch(ctx, "k_scan_small", k_scan_small<OffT>, 1, kBlock, 0, st, q, d_ctl, off, (OffT)m, sc, rs);
-    } else {
-        int nb = grid_for(F, kBlock, 1024);
-        launch(ctx, "k_scan_reduce", k_scan_reduce<OffT>, nb, kBlock, 0, st, q, (const TravCtl *)d_ctl, off, (OffT)m,
-               bsum);
-        launch(ctx, "k_scan_bsums", k_scan_bsums, 1, kBlock, 0, st, bsum, nb, d_ctl);
-        launch(ctx, "k_scan_write", k_scan_write<OffT>, nb, kBlock, 0, st, q, (const TravCtl *)d_ctl, off, (OffT)m,
-               (const unsigned long long *)bsum, sc, rs);
+    if (F <= kSmallFrontier) {  // the scan and the tile rows in one CTA
+        launch(ctx, "k_scan_small", k_scan_small<OffT>, 1, kBlock, 0, st, q, d_ctl, off, (OffT)m, sc, rs,
+               ws.tiles.as<uint32_t>());
+        return;
     }
+    int nb = grid_for(F, kBlock, 1024);
+    launch(ctx, "k_scan_reduce", k_scan_reduce<OffT>, nb, kBlock, 0, st, q, (const TravCtl *)d_ctl, off, (OffT)m,
+           bsum);
+    launch(ctx, "k_scan_bsums", k_scan_bsums, 1, kBlock, 0, st, bsum, nb, d_ctl);
+    launch(ctx, "k_scan_write", k_scan_write<OffT>, nb, kBlock, 0, st, q, (const TravCtl *)d_ctl, off, (OffT)m,
+           (const unsigned long long *)bsum, sc, rs);
     launch(ctx, "k_tile_rows", k_tile_rows<OffT>, sms * 4, kBlock, 0, st, (const OffT *)sc, (const TravCtl *)d_ctl,
            ws.tiles.as<uint32_t>());
 }

@@ -139,8 +139,9 @@ struct TravCtl {
     unsigned int error;           // nonzero: a kernel detected a bad index
     unsigned int bu_next;         // bottom-up BFS chunk counter (zero before each round)
     unsigned int bu_found;        // vertices a bottom-up round reached (its next frontier)
-    unsigned int pad[2];
-    unsigned long long frontier_E;  // unclipped edges of the current frontier (k_level_advance)
+    unsigned int compact_done;    // CTAs of the level's compaction that finished (the last ends the level)
+    unsigned int pad;
+    unsigned long long frontier_E;  // unclipped edges of the current frontier (set at the level's end)
 };
 
 // --------------------------------------------------------------------------

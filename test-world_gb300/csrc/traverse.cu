@@ -156,14 +156,61 @@ __device__ __forceinline__ uint32_t warp_bit_vertex(uint32_t word, uint32_t pre,
     return (uint32_t)((wd0 + lo) * 32 + __fns(w, 0, (int)(r - ex) + 1));
 }
 
-// After a pull round (skip_at below ~0) the kernel does nothing when the
+template <class OffT>
+__device__ __forceinline__ void compact_body(const uint32_t *bm, uint64_t words, uint32_t *q, TravCtl *ctl,
+                                             uint32_t *vis, uint32_t *far_bm, const OffT *off);
+
+// End of a level (so the host only reads the control block): the next
+// frontier's size and unclipped edge count become the current ones, the
+// per-level counters restart and the level value advances.  A pull round
+// whose finds were not compacted (skip_at or more of them) gives its own
+// count as the frontier size.  Run by the last CTA of k_compact.
+__device__ void level_advance(TravCtl *ctl, unsigned long long skip_at) {
+    uint32_t F = atomicExch(&ctl->next_tail, 0u);
+    const uint32_t found = atomicExch(&ctl->bu_found, 0u);
+    if (found >= skip_at) F = found;
+    ctl->F = F;
+    ctl->frontier_E = atomicExch(&ctl->next_E, 0ull);
+    ctl->bu_next = 0;
+    ctl->level_val += 1u;
+}
+
+// After a pull round (skip_at below ~0) the queue is not built when the
 // round found skip_at vertices or more: the next round pulls too and reads
-// only the bitmap.
+// only the bitmap.  `clear` (this level's frontier bitmap, read by nothing
+// after this kernel) is zeroed for reuse as the level after next's bitmap;
+// with `advance` the last CTA to finish ends the level (level_advance).
 template <class OffT>
 __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t *bm, uint64_t words, uint32_t *q,
                                                     TravCtl *ctl, uint32_t *vis, uint32_t *far_bm,
-                                                    const OffT *off, unsigned long long skip_at) {
-    if (ctl->bu_found >= skip_at) return;  // the same value in every thread
+                                                    const OffT *off, unsigned long long skip_at,
+                                                    uint32_t *clear, int advance) {
+    // read before any CTA can advance: the last one does so only after every
+    // CTA has passed here
+    const bool skip = ctl->bu_found >= skip_at;
+    if (clear)
+        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < words;
+             i += (uint64_t)gridDim.x * blockDim.x)
+            clear[i] = 0u;
+    if (!skip) compact_body<OffT>(bm, words, q, ctl, vis, far_bm, off);
+    if (advance) {
+        __syncthreads();  // this CTA's counter updates are issued
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(&ctl->compact_done, 1u) == gridDim.x - 1) {
+                __threadfence();
+                level_advance(ctl, skip_at);
+                ctl->compact_done = 0u;
+            }
+        }
+    }
+}
+
+// The queue of the set bits of bm (vertex order), its size appended to
+// ctl->next_tail and, with off, its unclipped edge count to ctl->next_E.
+template <class OffT>
+__device__ __forceinline__ void compact_body(const uint32_t *bm, uint64_t words, uint32_t *q, TravCtl *ctl,
+                                             uint32_t *vis, uint32_t *far_bm, const OffT *off) {
     unsigned long long degsum = 0;
     constexpr int kWarps = kBlock / 32;
     __shared__ uint32_t s_warp[kWarps];
@@ -228,23 +275,6 @@ __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t *bm, uint64_t
         degsum = block_reduce_sum(degsum);
         if (threadIdx.x == 0 && degsum) atomicAdd(&ctl->next_E, degsum);
     }
-}
-
-// End of a level, on the device (so the host only reads the control block):
-// the next frontier's size and unclipped edge count become the current
-// ones, the per-level counters restart and the level value advances.  A
-// pull round whose finds were not compacted (skip_at or more of them) gives
-// its own count as the frontier size.
-__global__ void k_level_advance(TravCtl *ctl, unsigned long long skip_at) {
-    uint32_t F = ctl->next_tail;
-    if (ctl->bu_found >= skip_at) F = ctl->bu_found;
-    ctl->F = F;
-    ctl->frontier_E = ctl->next_E;
-    ctl->next_tail = 0;
-    ctl->next_E = 0;
-    ctl->bu_next = 0;
-    ctl->bu_found = 0;
-    ctl->level_val += 1u;
 }
 
 // Load-balanced top-down expansion of the frontier's (resident) edges.
@@ -855,7 +885,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
                    (const TravCtl *)d_ctl);
             launch(ctx, "k_compact", k_compact<OffT>, compact_grid, kBlock, 0, st,
                    (const uint32_t *)ws.bm[cur].as<uint32_t>(), words, ws.q[cur].as<uint32_t>(), d_ctl,
-                   (uint32_t *)nullptr, (uint32_t *)nullptr, (const OffT *)nullptr, ~0ull);
+                   (uint32_t *)nullptr, (uint32_t *)nullptr, (const OffT *)nullptr, ~0ull, (uint32_t *)nullptr, 0);
             PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
             PTG_CUDA_TRY(cudaStreamSynchronize(st));
             F = h_ctl->next_tail;
@@ -869,7 +899,8 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         rr.iterations++;
         uint32_t *q_cur = ws.q[cur].as<uint32_t>(), *q_nxt = ws.q[cur ^ 1].as<uint32_t>();
         uint32_t *bm_cur = ws.bm[cur].as<uint32_t>(), *bm_nxt = ws.bm[cur ^ 1].as<uint32_t>();
-        PTG_CUDA_TRY(cudaMemsetAsync(bm_nxt, 0, words * 4, st));
+        // bm_nxt is clear: zeroed at the start, then by each level's
+        // compaction as the bitmap it had just finished with
         PushTargets pt{d_value, bm_nxt, use_far ? ws.farbm.as<uint32_t>() : nullptr, vis, d_ctl,
                        bfs_by_caller_id ? g->d_perm.as<uint32_t>() : nullptr};
         int scan_blocks = grid_for(F, kBlock, kScanBlocks);
@@ -893,8 +924,9 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
                    kBlock, 0, st, n, off, col, bm_cur, (const uint32_t *)g->d_nzbm.as<uint32_t>(), pt);
         } else {
             const bool small = F <= kSmallFrontier;
-            if (small) {
-                launch(ctx, "k_scan_small", k_scan_small<OffT>, 1, kBlock, 0, st, q_cur, d_ctl, off, clip, sc, rs);
+            uint32_t *tr = ws.tiles.as<uint32_t>();
+            if (small) {  // one CTA: the scan and the tile rows
+                launch(ctx, "k_scan_small", k_scan_small<OffT>, 1, kBlock, 0, st, q_cur, d_ctl, off, clip, sc, rs, tr);
             } else {
                 launch(ctx, "k_scan_reduce", k_scan_reduce<OffT>, scan_blocks, kBlock, 0, st, q_cur, d_ctl, off,
                        clip, bsum);
@@ -905,9 +937,9 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
             const int ecap = sms * (int)tu.expand_ctas_per_sm;
             int eg = ecap;
             if (allow_bu) eg = grid_for(E, kTile, ecap);
-            uint32_t *tr = ws.tiles.as<uint32_t>();
-            launch(ctx, "k_tile_rows", k_tile_rows<OffT>, allow_bu ? grid_for(E / kTile + 1, kBlock, sms * 4) : sms * 4,
-                   kBlock, 0, st, sc, d_ctl, tr);
+            if (!small)
+                launch(ctx, "k_tile_rows", k_tile_rows<OffT>,
+                       allow_bu ? grid_for(E / kTile + 1, kBlock, sms * 4) : sms * 4, kBlock, 0, st, sc, d_ctl, tr);
             if (kind == TRAV_BFS)
                 launch(ctx, "k_expand_bfs", k_expand<OffT, 0>, eg, kBlock, 0, st, q_cur, sc, rs, tr, col, wt, pt);
             else if (kind == TRAV_SSSP)
@@ -1021,8 +1053,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         launch(ctx, "k_compact", k_compact<OffT>, compact_grid, kBlock, 0, st, (const uint32_t *)bm_nxt, words, q_nxt,
                d_ctl, bottom_up ? (uint32_t *)nullptr : vis,
                use_far ? ws.farbm.as<uint32_t>() : (uint32_t *)nullptr,
-               allow_bu && !bottom_up ? off : (const OffT *)nullptr, skip_at);
-        launch(ctx, "k_level_advance", k_level_advance, 1, 1, 0, st, d_ctl, skip_at);
+               allow_bu && !bottom_up ? off : (const OffT *)nullptr, skip_at, bm_cur, 1);
         PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
         PTG_CUDA_TRY(cudaStreamSynchronize(st));
         PTG_REQUIRE(h_ctl->error == 0, PTG_ERR_CUDA, "frontier overflow in relax");
