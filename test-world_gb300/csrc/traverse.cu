@@ -621,20 +621,55 @@ __global__ void __launch_bounds__(kBlock) k_relax_partition(uint64_t e_begin, ui
             if (threadIdx.x == 0) s_off[nrows] = off[r0 + nrows];
         }
         __syncthreads();
-        for (uint64_t j = t0 + threadIdx.x; j < t1; j += kBlock) {
-            uint32_t uval;
-            if (staged) {
-                uint64_t row = last_le(s_off, 0, nrows, j);
-                uval = s_val[row];
-            } else {
-                uint64_t u = last_le(off, r0, r0 + nrows, j);
-                uval = part_active<MODE>(bm_cur, t, (uint32_t)u) ? t.value[u] : PTG_UNREACHED;
+        if (staged) {
+            // as k_expand: a thread's 8 consecutive edge slots, one search for
+            // the first slot's row, the rest by a register compare; all 8
+            // targets (and weights) loaded, then all 8 probes in flight (the
+            // value array of a graph that does not fit HBM is far larger than
+            // L2, so each probe is a DRAM round trip)
+            const uint32_t len = (uint32_t)(t1 - t0), s0 = threadIdx.x * kExpandPerThread;
+            if (s0 < len) {
+                const uint64_t j0 = t0 + s0;
+                uint32_t row = (uint32_t)last_le(s_off, 0, nrows, j0);
+                uint64_t next = (uint64_t)s_off[row + 1];
+                uint32_t uval = s_val[row];
+                uint32_t v[kExpandPerThread], nd[kExpandPerThread];
+#pragma unroll
+                for (int b = 0; b < kExpandPerThread; b++) {
+                    const uint64_t j = j0 + b;
+                    v[b] = PTG_UNREACHED;
+                    nd[b] = PTG_UNREACHED;
+                    if (s0 + b < len) {
+                        while (j >= next) {  // next row (skips zero-degree rows)
+                            row++;
+                            next = (uint64_t)s_off[row + 1];
+                            uval = s_val[row];
+                        }
+                        if (uval != PTG_UNREACHED) {
+                            const uint64_t le = j - e_begin;
+                            v[b] = __ldcs(stage_col + le);
+                            nd[b] = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + __ldcs(stage_w + le) : uval);
+                        }
+                    }
+                }
+                uint32_t cur[kExpandPerThread];
+#pragma unroll
+                for (int b = 0; b < kExpandPerThread; b++) cur[b] = v[b] != PTG_UNREACHED ? t.value[v[b]] : 0u;
+#pragma unroll
+                for (int b = 0; b < kExpandPerThread; b++)
+                    if (nd[b] < cur[b]) relax(t, v[b], nd[b], thr);
             }
-            if (uval == PTG_UNREACHED) continue;
-            uint64_t le = j - e_begin;
-            uint32_t v = __ldcs(stage_col + le);
-            uint32_t nd = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + __ldcs(stage_w + le) : uval);
-            relax_probe(t, v, nd, thr);
+        } else {
+            // more rows than slots (zero-degree rows): search each edge's row
+            for (uint64_t j = t0 + threadIdx.x; j < t1; j += kBlock) {
+                uint64_t u = last_le(off, r0, r0 + nrows, j);
+                uint32_t uval = part_active<MODE>(bm_cur, t, (uint32_t)u) ? t.value[u] : PTG_UNREACHED;
+                if (uval == PTG_UNREACHED) continue;
+                uint64_t le = j - e_begin;
+                uint32_t v = __ldcs(stage_col + le);
+                uint32_t nd = MODE == 0 ? uval + 1u : (MODE == 1 ? uval + __ldcs(stage_w + le) : uval);
+                relax_probe(t, v, nd, thr);
+            }
         }
         __syncthreads();
     }
