@@ -336,11 +336,11 @@ ptg_status ptg_ppr_batch(ptg_graph *g, const uint32_t *sources, uint32_t k, floa
  * CSR is checked on the device before any edge is read through it: offsets
  * that do not start at 0, decrease, or do not end at m, and targets >= n,
  * give PTG_ERR_INVALID (d_levels then holds no result).  The first call on a
- * device looks up the scratch's device address (make that first call before
- * any stream capture).  All calls share the scratch, so calls that overlap on
- * the GPU race: serialize them.  The call synchronizes `stream` once per BFS
- * level (it reads the next frontier's size back) and returns when the BFS has
- * finished on it. */
+ * device looks up the scratch's device address.  All calls share the scratch,
+ * so calls that overlap on the GPU race: serialize them.  The call
+ * synchronizes `stream` once per BFS level (it reads the next frontier's size
+ * back), so it cannot run inside a stream capture, and returns when the BFS
+ * has finished on it. */
 #define PTG_NOALLOC_MAX_VERTICES (1u << 20)
 #define PTG_NOALLOC_SCRATCH_BYTES ((16u << 20) + (64u << 10))
 ptg_status ptg_bfs_noalloc(const uint32_t *d_offsets, const uint32_t *d_col, uint32_t n,
