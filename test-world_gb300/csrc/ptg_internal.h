@@ -220,11 +220,26 @@ struct Prof {
 // --------------------------------------------------------------------------
 // context / graph
 // --------------------------------------------------------------------------
+// What the host reads at the end of an in-HBM traversal level, written by
+// the last CTA of the level's compaction straight into page-locked host
+// memory (device-mapped) and published by `seq`: the host polls it instead
+// of copying the control block back and synchronizing the stream.
+struct LevelMsg {
+    uint32_t seq;    // written last
+    uint32_t F;      // the next frontier's size
+    uint32_t error;  // TravCtl::error
+    uint32_t pad;
+    unsigned long long frontier_E;  // its unclipped edge count
+};
+
 struct Workspace {
     DevBuf value, q[2], bm[2], farbm, vis, scan, rowstart, tiles, bsum, ctl, aux, aux2, flags;
     DevBuf ms[3];  // multi-source 64-bit masks
     DevBuf relab[2];  // results in the stored vertex order, before mapping to caller ids
     PinnedBuf h_ctl, h_flags;
+    PinnedBuf h_msg;  // LevelMsg, mapped
+    LevelMsg *d_msg = nullptr;  // its device address (nullptr: not mapped, copy the control block)
+    uint32_t msg_seq = 0;
 };
 
 struct Graph;

@@ -39,6 +39,7 @@
 //    active adjacency into a unified-memory buffer the GPU page-faults on,
 //    main.cu:1126-1156, 1336-1378).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 
@@ -179,12 +180,14 @@ __device__ void level_advance(TravCtl *ctl, unsigned long long skip_at) {
 // round found skip_at vertices or more: the next round pulls too and reads
 // only the bitmap.  `clear` (this level's frontier bitmap, read by nothing
 // after this kernel) is zeroed for reuse as the level after next's bitmap;
-// with `advance` the last CTA to finish ends the level (level_advance).
+// with `advance` the last CTA to finish ends the level (level_advance) and,
+// given msg, publishes the level's outcome to the host (seq written last,
+// after a system-scope fence).
 template <class OffT>
 __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t *bm, uint64_t words, uint32_t *q,
                                                     TravCtl *ctl, uint32_t *vis, uint32_t *far_bm,
                                                     const OffT *off, unsigned long long skip_at,
-                                                    uint32_t *clear, int advance) {
+                                                    uint32_t *clear, int advance, LevelMsg *msg, uint32_t seq) {
     // read before any CTA can advance: the last one does so only after every
     // CTA has passed here
     const bool skip = ctl->bu_found >= skip_at;
@@ -201,6 +204,14 @@ __global__ void __launch_bounds__(kBlock) k_compact(const uint32_t *bm, uint64_t
                 __threadfence();
                 level_advance(ctl, skip_at);
                 ctl->compact_done = 0u;
+                if (msg) {
+                    volatile LevelMsg *m = msg;
+                    m->F = ctl->F;
+                    m->error = *(volatile unsigned int *)&ctl->error;
+                    m->frontier_E = ctl->frontier_E;
+                    __threadfence_system();
+                    m->seq = seq;
+                }
             }
         }
     }
@@ -783,6 +794,35 @@ void build_nonzero_bits(ptg_graph *g) {
            g->ctx->stream, g->d_off.as<OffT>(), g->n, g->d_nzbm.as<uint32_t>());
 }
 
+// The outcome of the level whose compaction was just queued (message
+// ws.msg_seq), read from mapped host memory once the compaction's last CTA
+// has published it.  While waiting, the stream is asked now and then
+// whether it has failed, or finished without the message; a level that
+// takes longer than ten minutes is reported as a timeout.
+LevelMsg wait_level_msg(Workspace &ws, cudaStream_t st) {
+    LevelMsg *m = ws.h_msg.as<LevelMsg>();
+    const uint32_t want = ws.msg_seq;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (uint64_t it = 1; __atomic_load_n(&m->seq, __ATOMIC_ACQUIRE) != want; it++) {
+        if (it % 1024 != 0) continue;
+        const cudaError_t e = cudaStreamQuery(st);
+        if (e == cudaSuccess) {
+            if (__atomic_load_n(&m->seq, __ATOMIC_ACQUIRE) == want) break;
+            throw Error{PTG_ERR_CUDA, "traversal level finished without publishing its outcome"};
+        }
+        if (e != cudaErrorNotReady) PTG_CUDA_TRY(e);
+        if (std::chrono::steady_clock::now() - t0 > std::chrono::minutes(10))
+            throw Error{PTG_ERR_TIMEOUT, "traversal level did not finish within ten minutes"};
+    }
+    LevelMsg out;
+    out.seq = want;
+    out.F = __atomic_load_n(&m->F, __ATOMIC_RELAXED);
+    out.error = __atomic_load_n(&m->error, __ATOMIC_RELAXED);
+    out.pad = 0;
+    out.frontier_E = __atomic_load_n(&m->frontier_E, __ATOMIC_RELAXED);
+    return out;
+}
+
 template <class OffT>
 void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value, uint32_t flags,
                    uint32_t delta, uint32_t max_iters, RunResult &rr) {
@@ -807,6 +847,17 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
     ws.bsum.ensure(kScanBlocks * 8);
     ws.ctl.ensure(sizeof(TravCtl));
     ws.h_ctl.ensure(sizeof(TravCtl));
+    if (!ws.h_msg.p) {
+        ws.h_msg.ensure(sizeof(LevelMsg));
+        std::memset(ws.h_msg.p, 0, sizeof(LevelMsg));
+        ws.msg_seq = 0;
+        void *dp = nullptr;
+        if (cudaHostGetDevicePointer(&dp, ws.h_msg.p, 0) == cudaSuccess) ws.d_msg = static_cast<LevelMsg *>(dp);
+        else cudaGetLastError();  // not mapped: the levels copy the control block back
+    }
+    // in-HBM levels hand their outcome over through mapped memory; streamed
+    // ones synchronize (their copy events are read after each level)
+    const bool poll = !g->out_of_core && ws.d_msg != nullptr;
     // Near/far buckets save edge work in HBM; a streamed graph is bound by the
     // host link, where every round re-copies its active partitions, so it
     // relaxes in label-correcting rounds unless a bucket width is asked for
@@ -920,7 +971,8 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
                    (const TravCtl *)d_ctl);
             launch(ctx, "k_compact", k_compact<OffT>, compact_grid, kBlock, 0, st,
                    (const uint32_t *)ws.bm[cur].as<uint32_t>(), words, ws.q[cur].as<uint32_t>(), d_ctl,
-                   (uint32_t *)nullptr, (uint32_t *)nullptr, (const OffT *)nullptr, ~0ull, (uint32_t *)nullptr, 0);
+                   (uint32_t *)nullptr, (uint32_t *)nullptr, (const OffT *)nullptr, ~0ull, (uint32_t *)nullptr, 0,
+                   (LevelMsg *)nullptr, 0u);
             PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
             PTG_CUDA_TRY(cudaStreamSynchronize(st));
             F = h_ctl->next_tail;
@@ -1088,10 +1140,26 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         launch(ctx, "k_compact", k_compact<OffT>, compact_grid, kBlock, 0, st, (const uint32_t *)bm_nxt, words, q_nxt,
                d_ctl, bottom_up ? (uint32_t *)nullptr : vis,
                use_far ? ws.farbm.as<uint32_t>() : (uint32_t *)nullptr,
-               allow_bu && !bottom_up ? off : (const OffT *)nullptr, skip_at, bm_cur, 1);
-        PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
-        PTG_CUDA_TRY(cudaStreamSynchronize(st));
-        PTG_REQUIRE(h_ctl->error == 0, PTG_ERR_CUDA, "frontier overflow in relax");
+               allow_bu && !bottom_up ? off : (const OffT *)nullptr, skip_at, bm_cur, 1,
+               poll ? ws.d_msg : (LevelMsg *)nullptr, ws.msg_seq + 1);
+        uint32_t level_error;
+        if (poll) {
+            // the level's outcome arrives in mapped host memory: no copy,
+            // no stream synchronization (the next level's launches queue
+            // behind the compaction's last CTA)
+            ws.msg_seq++;
+            const LevelMsg m = wait_level_msg(ws, st);
+            level_error = m.error;
+            F = m.F;
+            next_E = m.frontier_E;
+        } else {
+            PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
+            PTG_CUDA_TRY(cudaStreamSynchronize(st));
+            level_error = h_ctl->error;
+            F = h_ctl->F;
+            next_E = h_ctl->frontier_E;
+        }
+        PTG_REQUIRE(level_error == 0, PTG_ERR_CUDA, "frontier overflow in relax");
         if (link_open) {
             // the level's copies, first start to last end (the compute stream
             // waited on every one of them before the sync above)
@@ -1100,8 +1168,6 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
             rr.link_ms += lms;
             link_open = false;
         }
-        F = h_ctl->F;
-        next_E = h_ctl->frontier_E;
         if (use_far) far_nonempty = true;
         cur ^= 1;
     }
