@@ -704,6 +704,21 @@ __global__ void __launch_bounds__(kBlock) k_far_min(const uint32_t *far_bm, uint
     if (lane_id() == 0 && best != PTG_UNREACHED) atomicMin(&ctl->far_min, (unsigned long long)best);
 }
 
+// Near/far bucket advance on the device (in-HBM graphs): the far pile's
+// minimum restarts, k_far_min finds it, and the new threshold is set from it
+// (unchanged when the pile is empty: the split then moves nothing).
+__global__ void k_far_reset(TravCtl *ctl) {
+    ctl->far_min = ~0ull;
+    ctl->next_tail = 0u;
+}
+
+__global__ void k_far_threshold(TravCtl *ctl, uint32_t delta) {
+    const unsigned long long fm = ctl->far_min;
+    if (fm == ~0ull) return;
+    const unsigned long long t = fm + delta;
+    ctl->threshold = t >= PTG_UNREACHED ? PTG_UNREACHED : (uint32_t)t;
+}
+
 // Near/far: move the far vertices below the new threshold into the (empty)
 // near frontier bitmap; k_compact then builds its queue.
 __global__ void __launch_bounds__(kBlock) k_far_split(uint32_t *far_bm, uint64_t words,
@@ -951,6 +966,30 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
     while (true) {
         if (F == 0) {
             if (!use_far || !far_nonempty) break;
+            if (poll) {
+                // the bucket advance and the split's queue on the device, the
+                // new frontier's size through the level message (zero: the
+                // far pile was empty, since the split moves at least the
+                // vertex at the far minimum)
+                launch(ctx, "k_far_reset", k_far_reset, 1, 1, 0, st, d_ctl);
+                launch(ctx, "k_far_min", k_far_min, grid_for(words, kBlock, sms * 8), kBlock, 0, st,
+                       (const uint32_t *)ws.farbm.as<uint32_t>(), words, (const uint32_t *)d_value, d_ctl);
+                launch(ctx, "k_far_threshold", k_far_threshold, 1, 1, 0, st, d_ctl, delta);
+                launch(ctx, "k_far_split", k_far_split, grid_for(words, kBlock, sms * 8), kBlock, 0, st,
+                       ws.farbm.as<uint32_t>(), words, (const uint32_t *)d_value, ws.bm[cur].as<uint32_t>(),
+                       (const TravCtl *)d_ctl);
+                launch(ctx, "k_compact", k_compact<OffT>, compact_grid, kBlock, 0, st,
+                       (const uint32_t *)ws.bm[cur].as<uint32_t>(), words, ws.q[cur].as<uint32_t>(), d_ctl,
+                       (uint32_t *)nullptr, (uint32_t *)nullptr, (const OffT *)nullptr, ~0ull, (uint32_t *)nullptr, 1,
+                       ws.d_msg, ws.msg_seq + 1);
+                ws.msg_seq++;
+                const LevelMsg m = wait_level_msg(ws, st);
+                PTG_REQUIRE(m.error == 0, PTG_ERR_CUDA, "frontier overflow in relax");
+                F = m.F;
+                next_E = m.frontier_E;
+                if (F == 0) break;
+                continue;
+            }
             // advance the threshold past the smallest far distance
             unsigned long long big = ~0ull;
             PTG_CUDA_TRY(cudaMemcpyAsync(&d_ctl->far_min, &big, 8, cudaMemcpyHostToDevice, st));
