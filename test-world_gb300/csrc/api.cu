@@ -231,6 +231,49 @@ void place_hubs(ptg_graph *g, const std::vector<uint64_t> &off, uint64_t PE, cud
 }
 
 }  // namespace
+
+// The workspace's level message: page-locked host memory and its device
+// address (left null when the memory cannot be mapped: the loops then copy
+// the control block back).
+void ensure_level_msg(Workspace &ws) {
+    if (ws.h_msg.p) return;
+    ws.h_msg.ensure(sizeof(LevelMsg));
+    std::memset(ws.h_msg.p, 0, sizeof(LevelMsg));
+    ws.msg_seq = 0;
+    void *dp = nullptr;
+    if (cudaHostGetDevicePointer(&dp, ws.h_msg.p, 0) == cudaSuccess) ws.d_msg = static_cast<LevelMsg *>(dp);
+    else cudaGetLastError();
+}
+
+// The outcome of the level (or multi-source round) just queued (message
+// ws.msg_seq), read from mapped host memory once its last kernel has
+// published it.  While waiting, the stream is asked now and then
+// whether it has failed, or finished without the message; a level that
+// takes longer than ten minutes is reported as a timeout.
+LevelMsg wait_level_msg(Workspace &ws, cudaStream_t st) {
+    LevelMsg *m = ws.h_msg.as<LevelMsg>();
+    const uint32_t want = ws.msg_seq;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (uint64_t it = 1; __atomic_load_n(&m->seq, __ATOMIC_ACQUIRE) != want; it++) {
+        if (it % 1024 != 0) continue;
+        const cudaError_t e = cudaStreamQuery(st);
+        if (e == cudaSuccess) {
+            if (__atomic_load_n(&m->seq, __ATOMIC_ACQUIRE) == want) break;
+            throw Error{PTG_ERR_CUDA, "traversal level finished without publishing its outcome"};
+        }
+        if (e != cudaErrorNotReady) PTG_CUDA_TRY(e);
+        if (std::chrono::steady_clock::now() - t0 > std::chrono::minutes(10))
+            throw Error{PTG_ERR_TIMEOUT, "traversal level did not finish within ten minutes"};
+    }
+    LevelMsg out;
+    out.seq = want;
+    out.F = __atomic_load_n(&m->F, __ATOMIC_RELAXED);
+    out.error = __atomic_load_n(&m->error, __ATOMIC_RELAXED);
+    out.pad = 0;
+    out.frontier_E = __atomic_load_n(&m->frontier_E, __ATOMIC_RELAXED);
+    return out;
+}
+
 }  // namespace ptg
 
 extern "C" {

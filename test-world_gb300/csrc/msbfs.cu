@@ -514,6 +514,7 @@ void ms_prepare(ptg_graph *g, uint64_t mask_bytes) {
     ws.bsum.ensure(1024 * 8 + 256 * 4 + 3 * 32);
     ws.ctl.ensure(sizeof(TravCtl));
     ws.h_ctl.ensure(sizeof(TravCtl));
+    ensure_level_msg(ws);
 }
 
 // Chunked work items of the high-degree vertices, built once per graph.
@@ -543,22 +544,51 @@ void build_pull_items(ptg_graph *g) {
     g->pull_items_built = true;
 }
 
-// Read back the control block, take the new queue, reset counters.
+// End of a multi-source round on the device: the round's outcome goes to
+// the host through the level message (seq last, after a system-scope
+// fence) and the control block restarts with the new queue's size.
+__global__ void k_ms_round_end(TravCtl *ctl, LevelMsg *msg, uint32_t seq) {
+    TravCtl c = *ctl;
+    volatile LevelMsg *m = msg;
+    m->F = c.next_tail;
+    m->error = c.error;
+    m->frontier_E = c.m_unvisited;
+    m->E = c.E;
+    TravCtl upd{};
+    upd.F = c.next_tail;
+    *ctl = upd;
+    __threadfence_system();
+    m->seq = seq;
+}
+
+// The round's outcome (new queue size, unvisited edges, scanned edges),
+// then the new queue taken and the counters reset.  Through the mapped
+// level message when there is one, else by copying the control block back.
 inline void ms_next(ptg_ctx *ctx, Workspace &ws, uint64_t &F, uint64_t &Eact, uint64_t &E) {
     cudaStream_t st = ctx->stream;
     TravCtl *d_ctl = ws.ctl.as<TravCtl>(), *h_ctl = ws.h_ctl.as<TravCtl>();
-    PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
-    PTG_CUDA_TRY(cudaStreamSynchronize(st));
-    PTG_REQUIRE(h_ctl->error == 0, PTG_ERR_CUDA, "frontier overflow in multi-source round");
-    F = h_ctl->next_tail;
-    Eact = h_ctl->m_unvisited;
-    E = h_ctl->E;
+    if (ws.d_msg) {
+        launch(ctx, "k_ms_round_end", k_ms_round_end, 1, 1, 0, st, d_ctl, ws.d_msg, ws.msg_seq + 1);
+        ws.msg_seq++;
+        const LevelMsg msg = wait_level_msg(ws, st);
+        PTG_REQUIRE(msg.error == 0, PTG_ERR_CUDA, "frontier overflow in multi-source round");
+        F = msg.F;
+        Eact = msg.frontier_E;
+        E = msg.E;
+    } else {
+        PTG_CUDA_TRY(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(TravCtl), cudaMemcpyDeviceToHost, st));
+        PTG_CUDA_TRY(cudaStreamSynchronize(st));
+        PTG_REQUIRE(h_ctl->error == 0, PTG_ERR_CUDA, "frontier overflow in multi-source round");
+        F = h_ctl->next_tail;
+        Eact = h_ctl->m_unvisited;
+        E = h_ctl->E;
+        TravCtl upd{};
+        upd.F = (uint32_t)F;
+        PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &upd, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
+    }
     std::swap(ws.q[0].p, ws.q[1].p);
     std::swap(ws.q[0].bytes, ws.q[1].bytes);
     std::swap(ws.q[0].dev, ws.q[1].dev);
-    TravCtl upd{};
-    upd.F = (uint32_t)F;
-    PTG_CUDA_TRY(cudaMemcpyAsync(d_ctl, &upd, sizeof(TravCtl), cudaMemcpyHostToDevice, st));
 }
 
 template <class OffT, int W>

@@ -229,7 +229,8 @@ struct LevelMsg {
     uint32_t F;      // the next frontier's size
     uint32_t error;  // TravCtl::error
     uint32_t pad;
-    unsigned long long frontier_E;  // its unclipped edge count
+    unsigned long long frontier_E;  // its unclipped edge count (multi-source rounds: unvisited edges)
+    unsigned long long E;           // multi-source rounds: the round's scanned edges
 };
 
 struct Workspace {
@@ -241,6 +242,9 @@ struct Workspace {
     LevelMsg *d_msg = nullptr;  // its device address (nullptr: not mapped, copy the control block)
     uint32_t msg_seq = 0;
 };
+
+void ensure_level_msg(Workspace &ws);
+LevelMsg wait_level_msg(Workspace &ws, cudaStream_t st);
 
 struct Graph;
 

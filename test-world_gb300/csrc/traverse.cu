@@ -39,7 +39,6 @@
 //    active adjacency into a unified-memory buffer the GPU page-faults on,
 //    main.cu:1126-1156, 1336-1378).
 #include <algorithm>
-#include <chrono>
 #include <cmath>
 #include <cstring>
 
@@ -809,35 +808,6 @@ void build_nonzero_bits(ptg_graph *g) {
            g->ctx->stream, g->d_off.as<OffT>(), g->n, g->d_nzbm.as<uint32_t>());
 }
 
-// The outcome of the level whose compaction was just queued (message
-// ws.msg_seq), read from mapped host memory once the compaction's last CTA
-// has published it.  While waiting, the stream is asked now and then
-// whether it has failed, or finished without the message; a level that
-// takes longer than ten minutes is reported as a timeout.
-LevelMsg wait_level_msg(Workspace &ws, cudaStream_t st) {
-    LevelMsg *m = ws.h_msg.as<LevelMsg>();
-    const uint32_t want = ws.msg_seq;
-    const auto t0 = std::chrono::steady_clock::now();
-    for (uint64_t it = 1; __atomic_load_n(&m->seq, __ATOMIC_ACQUIRE) != want; it++) {
-        if (it % 1024 != 0) continue;
-        const cudaError_t e = cudaStreamQuery(st);
-        if (e == cudaSuccess) {
-            if (__atomic_load_n(&m->seq, __ATOMIC_ACQUIRE) == want) break;
-            throw Error{PTG_ERR_CUDA, "traversal level finished without publishing its outcome"};
-        }
-        if (e != cudaErrorNotReady) PTG_CUDA_TRY(e);
-        if (std::chrono::steady_clock::now() - t0 > std::chrono::minutes(10))
-            throw Error{PTG_ERR_TIMEOUT, "traversal level did not finish within ten minutes"};
-    }
-    LevelMsg out;
-    out.seq = want;
-    out.F = __atomic_load_n(&m->F, __ATOMIC_RELAXED);
-    out.error = __atomic_load_n(&m->error, __ATOMIC_RELAXED);
-    out.pad = 0;
-    out.frontier_E = __atomic_load_n(&m->frontier_E, __ATOMIC_RELAXED);
-    return out;
-}
-
 template <class OffT>
 void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value, uint32_t flags,
                    uint32_t delta, uint32_t max_iters, RunResult &rr) {
@@ -862,14 +832,7 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
     ws.bsum.ensure(kScanBlocks * 8);
     ws.ctl.ensure(sizeof(TravCtl));
     ws.h_ctl.ensure(sizeof(TravCtl));
-    if (!ws.h_msg.p) {
-        ws.h_msg.ensure(sizeof(LevelMsg));
-        std::memset(ws.h_msg.p, 0, sizeof(LevelMsg));
-        ws.msg_seq = 0;
-        void *dp = nullptr;
-        if (cudaHostGetDevicePointer(&dp, ws.h_msg.p, 0) == cudaSuccess) ws.d_msg = static_cast<LevelMsg *>(dp);
-        else cudaGetLastError();  // not mapped: the levels copy the control block back
-    }
+    ensure_level_msg(ws);
     // in-HBM levels hand their outcome over through mapped memory; streamed
     // ones synchronize (their copy events are read after each level)
     const bool poll = !g->out_of_core && ws.d_msg != nullptr;
