@@ -417,6 +417,14 @@ void ptg_ctx_destroy(ptg_ctx *ctx) {
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
+    for (int i = 0; i < 3; i++) {
+        if (ctx->side[i]) {
+            cudaStreamSynchronize(ctx->side[i]);
+            cudaStreamDestroy(ctx->side[i]);
+        }
+        if (ctx->side_join[i]) cudaEventDestroy(ctx->side_join[i]);
+    }
+    if (ctx->side_fork) cudaEventDestroy(ctx->side_fork);
     const int dev = ctx->device;
     const bool held = ctx->holds_cache;
     delete ctx;  // its buffers go to the device's block cache first

@@ -182,6 +182,19 @@ struct Prof {
         cudaEventRecord(cur.b, st);
         pending.push_back(cur);
     }
+    // A named span of stream work holding launches of its own (not counted
+    // as a launch), timed like one when profiling.
+    Rec span_begin(const char *name, cudaStream_t st) {
+        if (!enabled) return Rec{};
+        Rec r{name, get(), get()};
+        cudaEventRecord(r.a, st);
+        return r;
+    }
+    void span_end(const Rec &r, cudaStream_t st) {
+        if (!enabled || !r.a) return;
+        cudaEventRecord(r.b, st);
+        pending.push_back(r);
+    }
     // fold finished records into the totals (call after a synchronize)
     void resolve() {
         for (auto &r : pending) {
@@ -256,6 +269,10 @@ struct ptg_ctx {
     uint64_t hbm_bytes = 0;
     cudaStream_t stream = nullptr;       // compute stream
     cudaStream_t copy_stream = nullptr;  // host->device partition stream
+    // PageRank degree bins run side by side: streams forked from and joined
+    // back to `stream` every iteration (created on first use)
+    cudaStream_t side[3] = {nullptr, nullptr, nullptr};
+    cudaEvent_t side_fork = nullptr, side_join[3] = {nullptr, nullptr, nullptr};
     bool holds_cache = false;            // counted by the device block cache (devmem.cpp)
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     std::mutex mu;                       // one query at a time per context
