@@ -31,6 +31,11 @@
 //  * SSSP keeps a near frontier below a moving threshold and a far pile above
 //    it, so vertices are expanded close to their final distance instead of
 //    every time they improve (reference: Bellman-Ford rounds, main.cu:799-863).
+//  * Levels end on the device: the compaction's last CTA advances the
+//    control block and, for an in-HBM graph, writes what the host decides
+//    the next level from (frontier size, its edges, the error word) into
+//    device-mapped page-locked memory, which the host polls instead of
+//    copying the control block back and synchronizing the stream.
 //  * Out-of-core: edges past the resident prefix live in pinned host memory
 //    and are cut into fixed-size partitions.  Each round only partitions that
 //    hold an active vertex's edges are copied (cudaMemcpyAsync on a copy
@@ -1135,8 +1140,8 @@ void traverse_impl(ptg_graph *g, TravKind kind, uint32_t src, uint32_t *d_value,
         // found (and folded it into the visited bitmap); when the next round
         // pulls too (it stays pull unless the frontier is below n / beta)
         // nothing reads a queue, and the compaction skips itself on the
-        // device.  Then the control block advances on the device, and the
-        // host reads it once.
+        // device.  Its last CTA ends the level in the control block and,
+        // in HBM, publishes the outcome to the host (LevelMsg).
         const unsigned long long skip_at =
             bottom_up ? (unsigned long long)std::ceil((double)n / beta) : ~0ull;
         launch(ctx, "k_compact", k_compact<OffT>, compact_grid, kBlock, 0, st, (const uint32_t *)bm_nxt, words, q_nxt,
