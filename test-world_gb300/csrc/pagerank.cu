@@ -15,7 +15,9 @@
 // SpMV: rows are grouped once per graph by degree (a thread, 8 lanes or a
 // warp per row, and warp-sized chunks of the longest rows), each lane keeps
 // its own two-float partial, and partials meet through shuffles in a fixed
-// order, so the result of a row does not depend on scheduling.  The gathered
+// order, so the result of a row does not depend on scheduling.  The bins of
+// an iteration run side by side on streams forked from the context stream
+// (they read the same input and write disjoint rows).  The gathered
 // contributions of a scale-24 graph (67 MB) stay in L2; DRAM carries the
 // column stream, so the gathers' L2 sector traffic is the bound.
 #include <algorithm>

@@ -15,8 +15,12 @@
 // Build: two counting passes over contiguous vertex ranges (one warp each)
 // give a stable bucket order (perm: new -> caller id, newid: caller -> new);
 // a range scan gives the new offsets; rows are copied with mapped ids (short
-// and medium rows reordered by neighbour group, rows of 4096+ edges by whole
-// CTAs in the caller's order).
+// and medium rows reordered by neighbour group, rows of 4096+ edges in the
+// caller's order by whole CTAs).  All of that follows from the offsets, so a
+// graph given as host arrays is regrouped while its edges upload: pieces of
+// caller rows are copied to staging buffers on the copy stream and
+// regrouped from there, medium rows queued to a warp each and long rows cut
+// into 4096-edge items, so that no piece waits on one slow warp.
 #include <algorithm>
 #include <cmath>
 #include <vector>
