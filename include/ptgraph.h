@@ -237,7 +237,7 @@ typedef struct ptg_tuning {
                                     weight on graphs of 2^29+ edges, up to 4x wider on
                                     smaller ones (default 0.75; 0: label-correcting)     */
     uint32_t expand_ctas_per_sm; /* push relax (k_expand) CTAs per SM, 1..32 (default 4) */
-    uint32_t pr_ctas_per_sm;     /* PageRank SpMV CTAs per SM, 1..32 (default 8)         */
+    uint32_t pr_ctas_per_sm;     /* PageRank SpMV CTAs per SM, 1..32 (default 16)        */
     uint32_t pr_mid;             /* PageRank rows of 5..pr_mid edges run 8 lanes per
                                     row, longer ones a warp (default 256; 8..pr_chunk)   */
     uint32_t pr_chunk;           /* rows over pr_chunk edges are cut into pr_chunk-edge

@@ -330,7 +330,7 @@ void ptg_tuning_defaults(ptg_tuning *t) {
     t->bfs_beta = 18.f;
     t->sssp_delta_scale = 0.75f;
     t->expand_ctas_per_sm = 4;
-    t->pr_ctas_per_sm = 8;
+    t->pr_ctas_per_sm = 16;
     t->pr_mid = 256;
     t->pr_chunk = 4096;
     t->ms_pull_small = 32;

@@ -22,7 +22,7 @@ OFF_DEFAULT = {"bfs_alpha": 6.0, "bfs_beta": 36.0, "sssp_delta_scale": 0.5, "exp
 def test_builtin_values(ptg):
     d = ptg.tuning_defaults()
     assert d == {"bfs_alpha": 15.0, "bfs_beta": 18.0, "sssp_delta_scale": 0.75, "expand_ctas_per_sm": 4,
-                 "pr_ctas_per_sm": 8, "pr_mid": 256, "pr_chunk": 4096, "ms_pull_small": 32,
+                 "pr_ctas_per_sm": 16, "pr_mid": 256, "pr_chunk": 4096, "ms_pull_small": 32,
                  "ms_pull_chunk": 1024, "vertex_order": 1, "partition_bytes": 32 << 20}
     assert ptg.tuning_valid(d)
     assert ptg.tuning_valid(OFF_DEFAULT)
